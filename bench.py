@@ -1,0 +1,388 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 spectral-element time step.
+
+Default workload: the heterogeneous visco-elastic section (48x48x24 elements,
+lpd 4, three standard linear solids, seeded gradient + 5% perturbation model,
+per-element Q, one moment-tensor source, 64 surface receivers). A "step" is
+one time step of the whole section. `value` is GLL-point-updates/s
+(element-local points x steps x simulations / device seconds) over exactly K
+timed steps, measured with CUDA events on the library's own stream; the
+per-step working set (about 1.5 GB) is larger than L2, so no flush is needed.
+
+Also reported on the same line: the roofline of the dominant kernel (the
+element kernel; its algorithmic bytes over its event-timed duration), the
+end-to-end rate through the C ABI with host buffers, the FP32 error against
+the FP64 build, the oracle timed on the host cores, and SM clocks sampled
+during the timed region.
+
+--impl reference times the CPU implementation of the path instead: the
+reference is Fortran + MPI with no compiler on either machine, so the oracle's
+restatement of it runs on all host cores.
+
+With torchrun (N>1) every rank runs an independent replica of the workload
+(the path has no data-parallel split: every element lives on one GPU) and
+rank 0 prints the aggregate.
+"""
+import argparse
+import json
+import math
+import os
+import shutil
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path[:0] = [os.path.join(ROOT, "ses3d-nt_gb300"), os.path.join(ROOT, "oracle")]
+
+RANK = int(os.environ.get("RANK", "0"))
+WORLD = int(os.environ.get("WORLD_SIZE", "1"))
+LOCAL_RANK = int(os.environ.get("LOCAL_RANK", "0"))
+if WORLD > 1 and "CUDA_VISIBLE_DEVICES" not in os.environ:
+    # one GPU per rank; set before the library's first CUDA call
+    os.environ["CUDA_VISIBLE_DEVICES"] = str(LOCAL_RANK)
+
+METRIC = "GLL-point-updates/s"
+
+
+# ---------------------------------------------------------------------------
+# ranks (host-side only: barrier and reductions over gloo)
+# ---------------------------------------------------------------------------
+_pg = None
+
+
+def dist_init():
+    global _pg
+    if WORLD > 1 and _pg is None:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        os.environ.setdefault("MASTER_PORT", "29511")
+        dist.init_process_group("gloo", rank=RANK, world_size=WORLD)
+        _pg = dist
+    return _pg
+
+
+def barrier():
+    if WORLD > 1:
+        dist_init().barrier()
+
+
+def reduce(x, op):
+    """max / sum of a float over ranks (gloo)."""
+    if WORLD == 1:
+        return float(x)
+    import torch
+    d = dist_init()
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    d.all_reduce(t, op=d.ReduceOp.MAX if op == "max" else d.ReduceOp.SUM)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+        self.reader = None
+
+    def start(self):
+        exe = shutil.which("nvidia-smi")
+        if not exe:
+            return
+        self.proc = subprocess.Popen([exe, "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                                      "-lms", "200", "-i", str(self.device)],
+                                     stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        self.reader = threading.Thread(target=self._read, daemon=True)
+        self.reader.start()
+        time.sleep(0.3)
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.reader.join(timeout=2)
+        sm, smax, power, reasons = [], [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "power_w_max": max(power), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------
+def make_workload(name, nt_needed):
+    import workloads
+    if name == "config2":
+        wl = workloads.config2(nt=6000)
+    elif name == "config1":
+        wl = workloads.config1(nt=2000)
+    elif name == "config3":
+        wl = workloads.config3(nt=4000)
+    elif name == "config4":
+        wl = workloads.config4(nt=3000)
+    else:
+        raise SystemExit("unknown workload " + name)
+    wl.grid.nt = max(wl.grid.nt, nt_needed)
+    return wl
+
+
+def element_kernel_bytes(g, aniso=False):
+    """Algorithmic bytes of one element-kernel launch: stress R+W (48),
+    memory variables R+W (48 per mechanism), lambda+mu (8), tau (4, with
+    attenuation), A,B,C (12, anisotropic) per element-local point and the
+    velocity read (12) per unique point and simulation."""
+    e = g.precision // 4
+    S = g.batch
+    per_loc = (48 + 48 * g.n_sls) * S + 8 + (4 if g.n_sls else 0) + (12 if aniso else 0)
+    return (g.n_loc * per_loc + g.n_uni * 12 * S) * e
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_oracle_rate(wl, budget_s, max_steps=None, warm=2):
+    """Time the oracle (CPU restatement) on the workload's first simulation:
+    `warm` untimed steps, then steps until budget_s elapses."""
+    import sesnt_oracle
+    threads = sesnt_oracle.threads(os.cpu_count() or 1)
+    o = sesnt_oracle.Oracle(wl.grid, 4)
+    sesnt_oracle.load_workload(o, wl, sim=0)
+    o.run(warm)
+    n, t0 = 0, time.perf_counter()
+    while True:
+        o.run(1)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= budget_s or (max_steps and n >= max_steps):
+            break
+    o.close()
+    return wl.grid.n_loc * n / el, n, el, threads
+
+
+# ---------------------------------------------------------------------------
+# arms
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import numpy as np
+
+    import sesnt
+    import workloads
+
+    K, W = args.steps, args.warmup
+    KP = args.profile_steps
+    wl = make_workload(args.workload, W + K + KP + 1)
+    g = wl.grid
+    S = g.batch
+    hbm, peak_kind = peaks()
+
+    sim = sesnt.Simulation(g)
+    workloads.setup(sim, wl)
+    info = sim.info()
+    aniso = False
+    if W > 0:
+        sim.run(1, W)
+    sim.synchronize()
+
+    barrier()
+    clocks = Clocks(0)
+    clocks.start()
+    ms = sim.run_timed(W + 1, K)
+    clk = clocks.stop()
+    barrier()
+    ms_max = reduce(ms, "max")
+    units = float(g.n_loc) * K * S
+    total_units = reduce(units, "sum")
+    value = total_units / (ms_max / 1e3)
+
+    # per-kernel event timing of the same step sequence (dominant kernel)
+    prof = sim.run_profiled(W + K + 1, KP) if KP > 0 else None
+    seis_ok = bool(np.isfinite(sim.seismograms()).all())
+    sim.close()
+
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": WORLD, "steps": K, "warmup": W,
+        "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if g.precision == 4 else "f64",
+        "data": "synthetic: seeded (PCG64) gradient + 5% perturbation Earth model, per-element Q, "
+                "moment-tensor Ricker source",
+        "config": {"workload": wl.name, "elements": [g.nx, g.ny, g.nz], "lpd": g.lpd, "n_sls": g.n_sls,
+                   "batch": S, "dt": g.dt, "n_loc": g.n_loc, "n_uni": g.n_uni,
+                   "receivers": len(wl.receivers),
+                   "algorithmic_bytes_per_step": info["algorithmic_bytes_per_step"],
+                   "l2": "inputs larger than L2 (%.2f GB touched per step vs 0.13 GB L2)"
+                         % (info["algorithmic_bytes_per_step"] / 1e9),
+                   "graph": not (g.flags & sesnt.FLAG_NO_GRAPH),
+                   "parallelism": "replicas" if WORLD > 1 else "single GPU"},
+        "gpu_launches": int(K * info["launches_per_step"] + math.ceil(K / 32.0) + 1),
+        "clocks": clk,
+        "step_alg_hbm_gbs": info["algorithmic_bytes_per_step"] * K / (ms_max / 1e3) / 1e9,
+        "finite": seis_ok,
+    }
+    if prof is not None:
+        eb = element_kernel_bytes(g, aniso)
+        t_el = prof[0] / KP / 1e3
+        ach = eb / t_el / 1e9
+        line["kernels_ms_per_step"] = {"element": prof[0] / KP, "sources": prof[1] / KP, "node": prof[2] / KP,
+                                       "receivers": prof[3] / KP}
+        traffic = None
+        tr_path = os.path.join(ROOT, "profiles", "element_kernel_traffic.json")
+        if os.path.exists(tr_path):
+            try:
+                with open(tr_path) as f:
+                    tr = json.load(f)
+                if tr.get("workload") == wl.name:
+                    traffic = tr.get("dram_bytes_per_launch")
+            except Exception:
+                traffic = None
+        line["roofline"] = {"bound": "hbm", "kernel": "k_element", "achieved": ach, "peak": hbm,
+                            "peak_source": peak_kind, "unit": "GB/s", "frac": ach / hbm,
+                            "traffic": traffic, "alg_bytes_per_launch": eb}
+    if args.accuracy_steps > 0 and RANK == 0:
+        line["accuracy_vs_fp64"] = accuracy(args, wl)
+    if args.e2e and RANK == 0:
+        line["e2e"] = e2e(args, wl)
+    if RANK == 0 and WORLD == 1 and args.cpu_seconds > 0:
+        rate, n, el, threads = cpu_oracle_rate(wl, args.cpu_seconds)
+        line["cpu_baseline"] = {"value": rate, "unit": METRIC, "cores": threads, "kind": "port",
+                                "sample": "%d time steps of the full %s grid (oracle, %d OpenMP threads, %.1f s)"
+                                          % (n, wl.name, threads, el)}
+    return line
+
+
+def accuracy(args, wl):
+    """FP32 vs FP64 build of the same kernels: relative L2 of seismograms and
+    of the final vz over the first accuracy_steps steps."""
+    import copy
+
+    import numpy as np
+
+    import sesnt
+    import workloads
+    n = min(args.accuracy_steps, wl.grid.nt)
+    out = {}
+    res = {}
+    for prec in (4, 8):
+        w = copy.copy(wl)
+        w.grid = copy.copy(wl.grid)
+        w.grid.precision = prec
+        with sesnt.Simulation(w.grid) as sim:
+            workloads.setup(sim, w)
+            sim.run(1, n)
+            res[prec] = (sim.seismograms()[0].astype(np.float64), sim.field("vz", precision=8))
+    rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    out["steps"] = n
+    out["seismogram_rel_l2"] = rel(res[4][0], res[8][0])
+    out["vz_rel_l2"] = rel(res[4][1], res[8][1])
+    return out
+
+
+def e2e(args, wl):
+    """The drop-in call pattern through the C ABI with host buffers: create,
+    set_model from host arrays (H2D), register sources/receivers, then per
+    step sesnt_step(it) and a device-to-host read of that step's receiver
+    samples, for K steps."""
+    import numpy as np
+
+    import sesnt
+    import workloads
+    K = args.steps
+    g = wl.grid
+    model_bytes = sum(int(np.asarray(v).nbytes) for v in wl.model.values())
+    t0 = time.perf_counter()
+    sim = sesnt.Simulation(g)
+    workloads.setup(sim, wl)
+    buf = np.zeros((g.batch, len(wl.receivers), 3), np.float32)
+    for it in range(1, K + 1):
+        sim.step(it)
+        sim.samples(it, buf)
+    sim.synchronize()
+    el = time.perf_counter() - t0
+    sim.close()
+    return {"value": g.n_loc * K * g.batch / el, "unit": METRIC,
+            "h2d_bytes_per_step": model_bytes / K, "d2h_bytes_per_step": int(buf.nbytes),
+            "seconds": el, "includes": "handle create, model upload, source/receiver set-up, K x (step + D2H samples)"}
+
+
+def run_reference(args):
+    """CPU implementation of the path on the host cores (the oracle's
+    restatement of the Fortran reference), same workload and metric."""
+    if RANK != 0:
+        return None
+    K, W = args.steps, args.warmup
+    wl = make_workload(args.workload, W + K + 1)
+    budget = args.ref_seconds
+    rate, n, el, threads = cpu_oracle_rate(wl, budget, max_steps=K, warm=min(W, 2))
+    return {"impl": "reference", "metric": METRIC, "value": rate, "unit": METRIC, "n_gpus": WORLD, "steps": K,
+            "warmup": W, "ms_per_step": el / n * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (same seeded workload as the GPU arm)",
+            "config": {"workload": wl.name, "elements": [wl.grid.nx, wl.grid.ny, wl.grid.nz], "lpd": wl.grid.lpd,
+                       "n_sls": wl.grid.n_sls},
+            "cpu_baseline": {"value": rate, "unit": METRIC, "cores": threads, "kind": "port",
+                             "sample": "%d of %d requested time steps of the full grid after %d warm-up steps "
+                                       "(bounded to %.0f s); reference Fortran+MPI has no compiler here"
+                                       % (n, K, min(W, 2), budget)},
+            "e2e": {"value": rate, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="config2", choices=["config1", "config2", "config3", "config4"])
+    ap.add_argument("--profile-steps", type=int, default=20)
+    ap.add_argument("--accuracy-steps", type=int, default=1500)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-seconds", type=float, default=60.0)
+    ap.add_argument("--no-e2e", dest="e2e", action="store_false")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        raise SystemExit("--warmup must be >= 3")
+    line = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if RANK == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+    if _pg is not None:
+        _pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

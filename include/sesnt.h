@@ -1,0 +1,228 @@
+/*
+ * sesnt.h - C ABI of the GB300 spectral-element time step for Ses3d-NT.
+ *
+ * The reference drives one time step through argument-less module
+ * procedures and module globals:
+ *   - init_temp / ses3d_evolution        src/evolution.f90:48-84, 87-444
+ *   - model + auxiliary precompute      src/model_paras.F90:206-416
+ *   - geometry + taper precompute       src/geometric_paras.f90:108-325
+ *   - source_cls%add(it)                src/config/source.f90:359-370
+ *   - receiver_cls%record(it)           src/config/receiver.f90:136-142
+ *   - point location / Vandermonde      src/config/point.f90:150-254
+ * called from the forward loop at src/ses3d-nt.F90:240-270.
+ * This header replaces them with explicit, handle-based entry points that a
+ * Fortran driver binds through ISO_C_BINDING.
+ *
+ * Conventions
+ *   - Every function returns SESNT_OK (0) or a negative SESNT_E* code; the
+ *     library never aborts. sesnt_last_error() gives the message.
+ *   - Model and field arrays use the reference raw layout: Fortran order,
+ *     shape (nx, ny, nz, lpd+1, lpd+1, lpd+1), element x index fastest
+ *     (src/mpi_parallel_io.F90:61-110). The library copies inputs; callers
+ *     keep ownership of their buffers.
+ *   - A handle owns its device memory and one CUDA stream. Handles are not
+ *     thread-safe: use one handle per host thread.
+ *   - Time steps are numbered 1..nt as in the reference loop.
+ */
+#ifndef SESNT_H
+#define SESNT_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define SESNT_OK 0
+#define SESNT_EINVAL (-1)       /* invalid argument */
+#define SESNT_ECUDA (-2)        /* CUDA runtime error */
+#define SESNT_ENOMEM (-3)       /* device or host allocation failed */
+#define SESNT_ESTATE (-4)       /* call out of order (e.g. step before model) */
+#define SESNT_ERANGE (-5)       /* index or size out of range */
+#define SESNT_ETIMEOUT (-6)     /* a bounded device wait ran out */
+#define SESNT_ENOTFOUND (-7)    /* point outside the computational domain */
+#define SESNT_EUNSUPPORTED (-8) /* configuration not built into this library */
+#define SESNT_ENONFINITE (-9)   /* the wavefield contains NaN or Inf */
+
+/* flags (sesnt_grid_t.flags) */
+#define SESNT_FLAG_KAHAN 1u      /* compensated velocity update */
+#define SESNT_FLAG_NO_GRAPH 2u   /* sesnt_run launches kernels directly, no CUDA graph */
+
+/* source kinds (sesnt_add_source) */
+#define SESNT_SOURCE_MT 0 /* moment tensor: comp = Mxx Mxy Mxz Myy Myz Mzz */
+#define SESNT_SOURCE_SF 1 /* single force:  comp = fx fy fz (direction) */
+
+/* wavelets (sesnt_source_signature), src/misc/source_signature_mod.f90 */
+#define SESNT_WAVELET_DELTA 0
+#define SESNT_WAVELET_RICKER 1
+#define SESNT_WAVELET_GAUSS 2
+#define SESNT_WAVELET_SIN3 3
+#define SESNT_WAVELET_BRUNE 4
+
+/* receiver channels (sesnt_add_receiver), src/config/channel_mod.f90:505-592 */
+#define SESNT_CH_VX 1u
+#define SESNT_CH_VY 2u
+#define SESNT_CH_VZ 4u
+
+/* fields (sesnt_get_field) */
+#define SESNT_FIELD_VX 0
+#define SESNT_FIELD_VY 1
+#define SESNT_FIELD_VZ 2
+#define SESNT_FIELD_SXX 3 /* the reference's sxx_pml .. szz_pml */
+#define SESNT_FIELD_SXY 4
+#define SESNT_FIELD_SXZ 5
+#define SESNT_FIELD_SYY 6
+#define SESNT_FIELD_SYZ 7
+#define SESNT_FIELD_SZZ 8
+#define SESNT_FIELD_TAPER 9
+#define SESNT_FIELD_MASS 10     /* assembled mass matrix MM */
+#define SESNT_FIELD_MEMORY 13   /* + comp*3 + k: Mxx,Myy,Mzz,Mxy,Mxz,Myz x 3 mechanisms */
+
+typedef struct sesnt_handle sesnt_t;
+
+/* Grid, domain and time configuration. Field names and meanings follow the
+ * reference NAMELIST groups &grid, &model and &time
+ * (src/parser/parser.f90:45-69); the last four fields select the GPU build. */
+typedef struct sesnt_grid {
+    int nx, ny, nz;    /* global element counts (one domain, no partitions) */
+    int lpd;           /* Lagrange polynomial degree, 2..7 */
+    int taper_width;   /* absorbing taper width in elements */
+    float taper_slope; /* taper strength alpha */
+    float lat_min, lat_max, lon_min, lon_max; /* degrees */
+    float rad_min, rad_max;                   /* metres */
+    float dt;          /* time increment in seconds */
+    int nt;            /* number of time steps */
+    int n_sls;         /* 0 = elastic; 3 = three standard linear solids (needs q) */
+    int precision;     /* 4 = FP32 wavefields, 8 = FP64 wavefields */
+    int batch;         /* simulations sharing one Earth model (one per source), >= 1 */
+    unsigned flags;    /* SESNT_FLAG_* */
+} sesnt_grid_t;
+
+/* Replaces the set-up half of the reference driver (src/ses3d-nt.F90:84-160):
+ * configuration checks (src/config/config.F90:97-233), geometry and taper
+ * (src/geometric_paras.f90:108-325) and init_temp (src/evolution.f90:48-84).
+ * Allocates every device buffer the run needs. */
+int sesnt_create(const sesnt_grid_t *grid, sesnt_t **out);
+
+/* Frees the handle and its device memory. NULL is accepted. */
+int sesnt_destroy(sesnt_t *h);
+
+/* Message of the last failed call on this handle (or, when h is NULL, of the
+ * last failed handle-less call on this thread: sesnt_create,
+ * sesnt_locate_point). Never NULL. */
+const char *sesnt_last_error(const sesnt_t *h);
+
+/* Replaces make_model_parameters / read_model_parameters and
+ * init_auxiliary_model_parameters (src/model_paras.F90:97-137, 206-343,
+ * 389-416): copies the model (reference raw layout, float32), derives
+ * 2mu, kappa, tau, mu_tau and the assembled inverse mass matrix in FP64 on the
+ * device. a, b, c may be NULL (isotropic); q may be NULL (elastic). n_sls > 0
+ * requires q. Resets the wavefield. */
+int sesnt_set_model(sesnt_t *h, const float *rhoinv, const float *lambda, const float *mu, const float *a,
+                    const float *b, const float *c, const float *q);
+
+/* Replaces construct_point_cls (src/config/point.f90:150-254): maps
+ * (lat [deg], lon [deg], depth [m]) to element indices elem[3] (0-based ex,
+ * ey, ez) and the (lpd+1)^3 Vandermonde weights (Fortran order), in float32
+ * with the reference's formula order. Returns SESNT_EINVAL for invalid
+ * coordinates and SESNT_ENOTFOUND outside the domain. Host-only: needs no
+ * GPU and no handle. */
+int sesnt_locate_point(const sesnt_grid_t *grid, float lat, float lon, float depth, int elem[3], float *vanderm);
+
+/* Replaces make_source_signature_ for the built-in wavelets
+ * (src/config/source.f90:564-652, src/misc/source_signature_mod.f90:50-147):
+ * out[i] = wavelet(t = i*dt), i = 0..nt-1, float32. */
+int sesnt_source_signature(int wavelet, float onset, float width, float dt, int nt, float *out);
+
+/* Replaces create_from_source_mt / create_from_source_sf and source_cls%add
+ * (src/config/source.f90:215-370; channel_mod.f90:859-1095). Registers a
+ * source in simulation `sim` (0..batch-1) at element (ex,ey,ez) with
+ * Vandermonde weights `vanderm`. kind SESNT_SOURCE_MT takes comp[6] =
+ * Mxx Mxy Mxz Myy Myz Mzz; SESNT_SOURCE_SF takes comp[3] = fx fy fz.
+ * stf[nt] is the source-time function; channel data are stf*comp in float32.
+ * As in the reference, the value injected in step it+1 is the one set after
+ * step it (step 1 sees no source), and two sources in one element overwrite
+ * each other channel by channel (the later one wins). */
+int sesnt_add_source(sesnt_t *h, int sim, int ex, int ey, int ez, const float *vanderm, int kind,
+                     const float *comp, const float *stf, int nt);
+
+/* Replaces receiver_cls%record (src/config/receiver.f90:136-142,
+ * channel_mod.f90:505-592): registers a receiver at element (ex,ey,ez) with
+ * Vandermonde weights; channel_mask is a set of SESNT_CH_*. Every receiver is
+ * recorded in every simulation of the batch. Returns the receiver index
+ * (>= 0) or an error. */
+int sesnt_add_receiver(sesnt_t *h, int ex, int ey, int ez, const float *vanderm, unsigned channel_mask);
+
+/* One pass of the reference forward loop body for step `it` (1..nt):
+ * ses3d_evolution, then source add(it), then receiver record(it)
+ * (src/ses3d-nt.F90:240-250). Asynchronous on the handle's stream. */
+int sesnt_step(sesnt_t *h, int it);
+
+/* Steps it0 .. it0+nsteps-1. Long runs are replayed from a captured CUDA
+ * graph unless SESNT_FLAG_NO_GRAPH is set. Asynchronous. */
+int sesnt_run(sesnt_t *h, int it0, int nsteps);
+
+/* Same as sesnt_run, bracketed by CUDA events recorded on the handle's own
+ * stream; waits for completion and stores the elapsed milliseconds. */
+int sesnt_run_timed(sesnt_t *h, int it0, int nsteps, float *ms);
+
+/* Runs steps it0 .. it0+nsteps-1 with direct launches and CUDA events
+ * recorded on the handle's stream between the kernels of each step; stores
+ * the summed device milliseconds of the element, source, node and receiver
+ * kernels in ms[0..3]. Does the full work of sesnt_run. Synchronous. */
+int sesnt_run_profiled(sesnt_t *h, int it0, int nsteps, float ms[4]);
+
+/* Waits for all work queued on the handle. */
+int sesnt_synchronize(sesnt_t *h);
+
+/* Zeroes the wavefield, memory variables and seismograms (model kept). */
+int sesnt_reset(sesnt_t *h);
+
+/* Seismograms, float32 [batch][nrec][3][nt] with components vx, vy, vz
+ * (channels not requested at sesnt_add_receiver are zero). Synchronous. */
+int sesnt_get_seismograms(sesnt_t *h, float *out);
+
+/* The samples of step `it` (1..nt) of every receiver, float32
+ * [batch][nrec][3] (vx, vy, vz): what receiver_cls%record(it) stores on the
+ * host each step in the reference (src/config/receiver.f90:136-142).
+ * Synchronous; for a Fortran driver that keeps its own traces. */
+int sesnt_get_samples(sesnt_t *h, int it, float *out);
+
+/* Copies field `which` (SESNT_FIELD_*) of simulation `sim` to `out` in the
+ * reference raw layout (element-local copies of shared nodes included), as
+ * float32 (out_precision 4) or float64 (8). Synchronous. */
+int sesnt_get_field(sesnt_t *h, int sim, int which, void *out, int out_precision);
+
+/* Global minimum and maximum of the velocity components of simulation `sim`,
+ * the quantity the reference prints every step (v_ptp_glb,
+ * src/elastic_vars.F90:179-213). Returns SESNT_ENONFINITE if any value is
+ * NaN or Inf. Synchronous. */
+int sesnt_v_ptp(sesnt_t *h, int sim, float out[2]);
+
+/* Sums an element-local field over every copy of each shared GLL point and
+ * writes the sum back to every copy: the effect of
+ * communicate_local_boundaries (src/communicate_fields.F90:48-79) on one
+ * rank, done on the device through the library's unique-point numbering.
+ * field is float32 in the reference raw layout; in place. Synchronous. */
+int sesnt_assemble_field(sesnt_t *h, float *field);
+
+/* Sizes: out[0] elements, out[1] element-local GLL points (N_loc), out[2]
+ * unique GLL points (N_uni), out[3] device bytes held by the handle,
+ * out[4] algorithmic HBM bytes of one time step (whole batch),
+ * out[5] device kernel launches per time step. */
+int sesnt_info(const sesnt_t *h, long long out[6]);
+
+/* Device bytes sesnt_create + sesnt_set_model would allocate for `grid`
+ * (used by a scheduler to admit work by HBM footprint). */
+long long sesnt_footprint_bytes(const sesnt_grid_t *grid);
+
+/* The stream the handle launches on (cudaStream_t), for callers that order
+ * their own work after the library's. */
+void *sesnt_stream(const sesnt_t *h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SESNT_H */

@@ -1,0 +1,71 @@
+"""Builds libsesnt.so (the GB300 time step behind include/sesnt.h) in place.
+
+Host set-up code is compiled with g++ and -ffp-contract=off so its float32
+arithmetic matches the reference's rounding on x86-64 and aarch64 alike; the
+CUDA translation units are compiled for sm_103a only. Translation units are
+compiled in parallel.
+"""
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(HERE, "libsesnt.so")
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def _nvcc():
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", shutil.which("nvcc")):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError("nvcc not found")
+
+
+def _run(cmd):
+    p = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True)
+    if p.returncode != 0:
+        raise RuntimeError("command failed: %s\n%s" % (" ".join(cmd), p.stdout))
+    return p.stdout
+
+
+def sources():
+    cu = sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
+    cpp = sorted(f for f in os.listdir(CSRC) if f.endswith(".cpp"))
+    return cu, cpp
+
+
+def build(verbose=False, extra_nvcc=()):
+    """Compile every translation unit and link libsesnt.so. Returns its path."""
+    os.makedirs(BUILD, exist_ok=True)
+    nvcc = _nvcc()
+    cu, cpp = sources()
+    jobs = []
+    for f in cu:
+        obj = os.path.join(BUILD, f + ".o")
+        jobs.append(([nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-I", INCLUDE,
+                      "-Xcompiler", "-fPIC,-ffp-contract=off", *extra_nvcc,
+                      "-c", os.path.join(CSRC, f), "-o", obj], obj))
+    for f in cpp:
+        obj = os.path.join(BUILD, f + ".o")
+        jobs.append((["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall",
+                      "-I", INCLUDE, "-I", "/usr/local/cuda/include",
+                      "-c", os.path.join(CSRC, f), "-o", obj], obj))
+    with cf.ThreadPoolExecutor(max_workers=max(2, os.cpu_count() or 2)) as ex:
+        outs = list(ex.map(lambda j: _run(j[0]), jobs))
+    if verbose:
+        for o in outs:
+            if o.strip():
+                print(o)
+    objs = [o for _, o in jobs]
+    _run([nvcc, *ARCH, "-shared", "-o", LIB + ".tmp", *objs, "-Xcompiler", "-fPIC"])
+    os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

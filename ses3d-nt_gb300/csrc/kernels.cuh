@@ -1,0 +1,592 @@
+// sm_103a kernels of the spectral-element time step, templated on the
+// polynomial degree N (lpd), the wavefield precision T, the number of
+// standard linear solids and anisotropy. One translation unit per degree
+// instantiates them (kern_lpd<N>.cu).
+//
+// Per step (src/evolution.f90:87-444 followed by the driver's add/record,
+// src/ses3d-nt.F90:240-250):
+//   k_element  one thread per element-local GLL point, EPB elements per block:
+//              gather v of the element's points from the unique-point array
+//              into shared memory; nine line contractions for the velocity
+//              gradient (:130-159); spherical completion and symmetrisation
+//              (:165-173, :206-208); stress rate and integration (:287-311),
+//              or the standard-linear-solid form with its memory variables
+//              (:216-284, :415-442); taper of the stored stress (:404-409);
+//              the weak divergence (:332-367) as nine transposed line
+//              contractions over metric-weighted stresses in shared memory;
+//              assembly by atomic adds into the unique-point force
+//              (replaces :372-388 and src/communicate_fields.F90:48-247).
+//   k_sources  the moment-tensor / single-force slabs (channel_mod.f90:859-1095)
+//              pushed through the same weak divergence, added to the force.
+//   k_node     one thread per unique point: v += dt * F / M, taper
+//              (:393-402), force reset for the next step.
+//   k_receivers one warp per receiver: Lagrange interpolation of v
+//              (channel_mod.f90:505-592).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "sesnt_internal.h"
+
+namespace sesnt {
+
+template <int N>
+struct ElemCfg {
+    static constexpr int P = N + 1;
+    static constexpr int NP = P * P * P;
+    // elements per block: enough points to fill whole warps with little waste
+    static constexpr int EPB = NP <= 32 ? 8 : (NP <= 64 ? 2 : (NP <= 128 ? 2 : 1));
+    static constexpr int NT = ((EPB * NP + 31) / 32) * 32;
+};
+
+template <typename T>
+__device__ __forceinline__ T ld_stream(const T *p) {
+    return __ldcs(p);
+}
+template <typename T>
+__device__ __forceinline__ void st_stream(T *p, T v) {
+    __stcs(p, v);
+}
+
+// Taper from the three damping profiles (src/geometric_paras.f90:308-316):
+// corner normalisation, then exp(-0.1*prof^2).
+template <typename T>
+__device__ __forceinline__ T taper_value(T px, T py, T pz, T alpha) {
+    T prof = px + py + pz;
+    T den = T(1) + prof / alpha;
+    T qx = T(2) * px / den, qy = T(2) * py / den, qz = T(2) * pz / den;
+    T p2 = qx + qy + qz;
+    if (p2 == T(0)) return T(1);
+    return exp(-(T(0.1) * (p2 * p2)));
+}
+
+template <int N, typename T, int NSLS, bool ANISO>
+__global__ void __launch_bounds__(ElemCfg<N>::NT) k_element(const StepArgs<T> a) {
+    constexpr int P = ElemCfg<N>::P, NP = ElemCfg<N>::NP, EPB = ElemCfg<N>::EPB, NT = ElemCfg<N>::NT;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sD = reinterpret_cast<T *>(smem_raw);  // [4][P*P]
+    T *sv = sD + 4 * P * P;                   // [EPB][3][NP]
+    T *sf = sv + EPB * 3 * NP;                // [EPB][9][NP]
+
+    const int S = a.S;
+    const int s = blockIdx.x % S;
+    const int g = blockIdx.x / S;
+    const int t = threadIdx.x;
+    for (int x = t; x < 4 * P * P; x += NT) sD[x] = a.tabD[x];
+
+    const int le = t / NP;
+    const int p = t - le * NP;
+    const int e = g * EPB + le;
+    const bool act = (le < EPB) && (e < a.nel);
+    const int i = p % P, j = (p / P) % P, k = p / (P * P);
+    int ex = 0, ey = 0, ez = 0;
+    size_t u = 0;
+    const size_t nuni = (size_t)a.nuni, nloc = (size_t)a.nloc;
+    T vx = 0, vy = 0, vz = 0;
+    if (act) {
+        ex = e % a.nx;
+        ey = (e / a.nx) % a.ny;
+        ez = e / (a.nx * a.ny);
+        u = (size_t)(ex * N + i) + (size_t)a.NXU * ((size_t)(ey * N + j) + (size_t)a.NYU * (size_t)(ez * N + k));
+        const T *vs = a.v + (size_t)s * 3 * nuni;
+        vx = vs[u];
+        vy = vs[nuni + u];
+        vz = vs[2 * nuni + u];
+        T *my = sv + le * 3 * NP;
+        my[p] = vx;
+        my[NP + p] = vy;
+        my[2 * NP + p] = vz;
+    }
+    __syncthreads();
+
+    T fx = 0, fy = 0, fz = 0;
+    if (act) {
+        const T *Dx = sD, *Dy = sD + P * P, *Dz = sD + 2 * P * P;
+        const T *svx = sv + le * 3 * NP, *svy = svx + NP, *svz = svx + 2 * NP;
+        // velocity gradient: line contractions along the three GLL directions
+        T exx = 0, exy = 0, exz = 0, eyy = 0, eyx = 0, eyz = 0, ezz = 0, ezy = 0, ezx = 0;
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            const int px_ = q + P * (j + P * k);
+            const int py_ = i + P * (q + P * k);
+            const int pz_ = i + P * (j + P * q);
+            const T dx = Dx[q * P + i], dy = Dy[q * P + j], dz = Dz[q * P + k];
+            exx += svx[px_] * dx;
+            exy += svy[px_] * dx;
+            exz += svz[px_] * dx;
+            eyy += svy[py_] * dy;
+            eyx += svx[py_] * dy;
+            eyz += svz[py_] * dy;
+            ezz += svz[pz_] * dz;
+            ezy += svy[pz_] * dz;
+            ezx += svx[pz_] * dz;
+        }
+        // spherical completion (theta = x, phi = y, r = z)
+        const T rr = a.r[ez * P + k];
+        const T st = a.sin_t[ex * P + i], ct = a.cot_t[ex * P + i];
+        const T rs = rr * st;
+        ezz = -ezz;
+        eyy = eyy / rs + (vz + vx * ct) / rr;
+        exx = (vz + exx) / rr;
+        ezx = -ezx;
+        exz = (exz - vx) / rr;
+        ezy = -ezy;
+        eyz = -vy / rr + eyz / rs;
+        exy = exy / rr;
+        eyx = -(vy * ct) / rr + eyx / rs;
+        exy = (exy + eyx) * T(0.5);
+        exz = (exz + ezx) * T(0.5);
+        eyz = (eyz + ezy) * T(0.5);
+
+        // stress rates
+        const size_t li = (size_t)e * NP + p;
+        const T lam = ld_stream(a.lam + li), mu = ld_stream(a.mu + li);
+        T cA = 0, cB = 0, cC = 0;
+        if constexpr (ANISO) {
+            cA = ld_stream(a.A + li);
+            cB = ld_stream(a.B + li);
+            cC = ld_stream(a.C + li);
+        }
+        const T two_mu = T(2) * mu;
+        const T tr = exx + eyy + ezz;
+        T rxx, ryy, rzz, rxy, rxz, ryz;
+        T *sig = a.sig + (size_t)s * 6 * nloc + li;
+        if constexpr (NSLS > 0) {
+            const T tau = ld_stream(a.tau + li);
+            const T mu_tau = (T(1) + tau) * mu;
+            const T kappa = lam + two_mu / T(3);
+            T *mem = a.mem + (size_t)s * 6 * NSLS * nloc + li;
+            T m[6][NSLS];
+#pragma unroll
+            for (int c = 0; c < 6; ++c)
+#pragma unroll
+                for (int q = 0; q < NSLS; ++q) m[c][q] = ld_stream(mem + (size_t)(c * NSLS + q) * nloc);
+            T sm[6];
+#pragma unroll
+            for (int c = 0; c < 6; ++c) {
+                T acc = 0;
+#pragma unroll
+                for (int q = 0; q < NSLS; ++q) acc += m[c][q];
+                sm[c] = acc;
+            }
+            const T L = (kappa - T(2) * mu_tau / T(3)) * tr - two_mu * (sm[0] + sm[1] + sm[2]) / T(3);
+            const T tmt = T(2) * mu_tau;
+            rxx = L + tmt * exx + two_mu * sm[0];
+            ryy = L + tmt * eyy + two_mu * sm[1];
+            rzz = L + tmt * ezz + two_mu * sm[2];
+            rxy = tmt * exy + two_mu * sm[3];
+            rxz = tmt * exz + two_mu * sm[4];
+            ryz = tmt * eyz + two_mu * sm[5];
+            // memory variables (after the stress update, with this step's rates)
+            const T er[6] = {exx, eyy, ezz, exy, exz, eyz};
+#pragma unroll
+            for (int q = 0; q < NSLS; ++q) {
+                const T tp = a.tau_p[q];
+                const T Lq = a.dt * tau / (T(NSLS) * tp);
+#pragma unroll
+                for (int c = 0; c < 6; ++c) {
+                    const T mv = m[c][q];
+                    st_stream(mem + (size_t)(c * NSLS + q) * nloc, mv - a.dt * mv / tp - Lq * er[c]);
+                }
+            }
+        } else {
+            const T L = lam * tr;
+            rxx = L + two_mu * exx;
+            ryy = L + two_mu * eyy;
+            rzz = L + two_mu * ezz;
+            rxy = two_mu * exy;
+            rxz = two_mu * exz;
+            ryz = two_mu * eyz;
+        }
+        if constexpr (ANISO) {
+            rxx += cC * ezz + cA * (eyy + exx);
+            ryy += cC * ezz + cA * (eyy + exx);
+            rzz += cC * (eyy + exx);
+            rxz += T(2) * cB * exz;
+            ryz += T(2) * cB * eyz;
+        }
+        // integrate, taper the stored stress
+        const T sxx = ld_stream(sig) + a.dt * rxx;
+        const T sxy = ld_stream(sig + nloc) + a.dt * rxy;
+        const T sxz = ld_stream(sig + 2 * nloc) + a.dt * rxz;
+        const T syy = ld_stream(sig + 3 * nloc) + a.dt * ryy;
+        const T syz = ld_stream(sig + 4 * nloc) + a.dt * ryz;
+        const T szz = ld_stream(sig + 5 * nloc) + a.dt * rzz;
+        const T tp = taper_value(a.px[ex * P + i], a.py[ey * P + j], a.pz[ez * P + k], a.alpha);
+        st_stream(sig, sxx * tp);
+        st_stream(sig + nloc, sxy * tp);
+        st_stream(sig + 2 * nloc, sxz * tp);
+        st_stream(sig + 3 * nloc, syy * tp);
+        st_stream(sig + 4 * nloc, syz * tp);
+        st_stream(sig + 5 * nloc, szz * tp);
+
+        // metric-weighted fluxes for the weak divergence
+        const T W = a.w[i] * a.w[j] * a.w[k];
+        const T gx = W * rs * a.c1;
+        const T gy = W * rr * a.c2;
+        const T gz = W * (rr * rs) * a.c3;
+        T *my = sf + le * 9 * NP;
+        my[0 * NP + p] = sxx * gx;
+        my[1 * NP + p] = sxy * gy;
+        my[2 * NP + p] = sxz * gz;
+        my[3 * NP + p] = sxy * gx;
+        my[4 * NP + p] = syy * gy;
+        my[5 * NP + p] = syz * gz;
+        my[6 * NP + p] = sxz * gx;
+        my[7 * NP + p] = syz * gy;
+        my[8 * NP + p] = szz * gz;
+    }
+    __syncthreads();
+    if (act) {
+        const T *Dt = sD + 3 * P * P;
+        const T *my = sf + le * 9 * NP;
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            const int px_ = q + P * (j + P * k);
+            const int py_ = i + P * (q + P * k);
+            const int pz_ = i + P * (j + P * q);
+            const T di = Dt[i * P + q], dj = Dt[j * P + q], dk = Dt[k * P + q];
+            fx += my[2 * NP + pz_] * dk + my[1 * NP + py_] * dj + my[0 * NP + px_] * di;
+            fy += my[5 * NP + pz_] * dk + my[4 * NP + py_] * dj + my[3 * NP + px_] * di;
+            fz += my[8 * NP + pz_] * dk + my[7 * NP + py_] * dj + my[6 * NP + px_] * di;
+        }
+        T *F = a.F + (size_t)s * 3 * nuni;
+        atomicAdd(F + u, fx);
+        atomicAdd(F + nuni + u, fy);
+        atomicAdd(F + 2 * nuni + u, fz);
+    }
+}
+
+// Source slabs through the weak divergence, one block per resolved
+// (simulation, element) record. The slab set after step it-1 acts in step it
+// (src/ses3d-nt.F90:240-250), so step 1 injects nothing.
+template <int N, typename T>
+__global__ void __launch_bounds__(((ElemCfg<N>::NP + 31) / 32) * 32) k_sources(const StepArgs<T> a) {
+    constexpr int P = ElemCfg<N>::P, NP = ElemCfg<N>::NP;
+    const int it = *a.d_it + a.step_off;
+    if (it < 2) return;
+    const int di = it - 2;  // data(it-1), 0-based
+    __shared__ T sf[9 * NP];
+    __shared__ T sD[P * P];
+    const SrcRec rec = a.src[blockIdx.x];
+    const int t = threadIdx.x;
+    for (int x = t; x < P * P; x += blockDim.x) sD[x] = a.tabD[3 * P * P + x];
+    const int p = t;
+    const bool act = p < NP;
+    const int i = p % P, j = (p / P) % P, k = p / (P * P);
+    const int e = rec.elem;
+    const int ex = e % a.nx, ey = (e / a.nx) % a.ny, ez = e / (a.nx * a.ny);
+    T f0[3] = {0, 0, 0};
+    if (act) {
+        const T rr = a.r[ez * P + k];
+        const T rs = rr * a.sin_t[ex * P + i];
+        const T W = a.w[i] * a.w[j] * a.w[k];
+        const T rr2 = rr * rs;
+        T m[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            m[c] = 0;
+            if (rec.vm[c] >= 0) {
+                const T d = a.src_data[(size_t)rec.data[c] * a.nt + di];
+                m[c] = (-d * a.src_vm[(size_t)rec.vm[c] * NP + p]) / (a.jac * W * rr2);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+            if (rec.vm[6 + c] >= 0) {
+                const T d = a.src_data[(size_t)rec.data[6 + c] * a.nt + di];
+                f0[c] = -d * a.src_vm[(size_t)rec.vm[6 + c] * NP + p];
+            }
+        const T gx = W * rs * a.c1, gy = W * rr * a.c2, gz = W * rr2 * a.c3;
+        // m = xx, xy, xz, yy, yz, zz
+        sf[0 * NP + p] = m[0] * gx;
+        sf[1 * NP + p] = m[1] * gy;
+        sf[2 * NP + p] = m[2] * gz;
+        sf[3 * NP + p] = m[1] * gx;
+        sf[4 * NP + p] = m[3] * gy;
+        sf[5 * NP + p] = m[4] * gz;
+        sf[6 * NP + p] = m[2] * gx;
+        sf[7 * NP + p] = m[4] * gy;
+        sf[8 * NP + p] = m[5] * gz;
+    }
+    __syncthreads();
+    if (!act) return;
+    T fx = f0[0], fy = f0[1], fz = f0[2];
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+        const int px_ = q + P * (j + P * k);
+        const int py_ = i + P * (q + P * k);
+        const int pz_ = i + P * (j + P * q);
+        const T dI = sD[i * P + q], dJ = sD[j * P + q], dK = sD[k * P + q];
+        fx += sf[2 * NP + pz_] * dK + sf[1 * NP + py_] * dJ + sf[0 * NP + px_] * dI;
+        fy += sf[5 * NP + pz_] * dK + sf[4 * NP + py_] * dJ + sf[3 * NP + px_] * dI;
+        fz += sf[8 * NP + pz_] * dK + sf[7 * NP + py_] * dJ + sf[6 * NP + px_] * dI;
+    }
+    const size_t nuni = (size_t)a.nuni;
+    const size_t u =
+        (size_t)(ex * N + i) + (size_t)a.NXU * ((size_t)(ey * N + j) + (size_t)a.NYU * (size_t)(ez * N + k));
+    T *F = a.F + (size_t)rec.sim * 3 * nuni;
+    atomicAdd(F + u, fx);
+    atomicAdd(F + nuni + u, fy);
+    atomicAdd(F + 2 * nuni + u, fz);
+}
+
+// Decode a unique point into the element-local copy with the lowest element
+// index along each axis (the copy whose 1-D tables the node kernel reads).
+template <int N>
+__device__ __forceinline__ void unique_to_local(unsigned g, int ne, int &e, int &n) {
+    e = min((int)(g / N), ne - 1);
+    n = (int)g - e * N;
+}
+
+template <int N, typename T, bool KAHAN>
+__global__ void __launch_bounds__(256) k_node(const StepArgs<T> a) {
+    constexpr int P = N + 1;
+    const unsigned u = blockIdx.x * 256u + threadIdx.x;
+    const int s = blockIdx.y;
+    if (u >= (unsigned)a.nuni) return;
+    const unsigned gx = u % (unsigned)a.NXU, rest = u / (unsigned)a.NXU;
+    const unsigned gy = rest % (unsigned)a.NYU, gz = rest / (unsigned)a.NYU;
+    int ex, i, ey, j, ez, k;
+    unique_to_local<N>(gx, a.nx, ex, i);
+    unique_to_local<N>(gy, a.ny, ey, j);
+    unique_to_local<N>(gz, a.nz, ez, k);
+    const T tp = taper_value(a.px[ex * P + i], a.py[ey * P + j], a.pz[ez * P + k], a.alpha);
+    const T im = a.invM[u];
+    const size_t nuni = (size_t)a.nuni;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const size_t idx = ((size_t)s * 3 + c) * nuni + u;
+        const T f = a.F[idx];
+        a.F[idx] = T(0);
+        const T acc = f * im;
+        if constexpr (KAHAN) {
+            // Kahan-compensated v += dt*acc (the compensation is tapered with v)
+            const T vold = a.v[idx];
+            const T y = a.dt * acc - a.vc[idx];
+            const T tsum = vold + y;
+            const T comp = (tsum - vold) - y;
+            a.v[idx] = tsum * tp;
+            a.vc[idx] = comp * tp;
+        } else {
+            a.v[idx] = (a.v[idx] + a.dt * acc) * tp;
+        }
+    }
+}
+
+template <int N, typename T>
+__global__ void __launch_bounds__(128) k_receivers(const StepArgs<T> a) {
+    constexpr int P = N + 1, NP = P * P * P;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r = blockIdx.x * 4 + warp;
+    const int s = blockIdx.y;
+    if (r >= a.nrec) return;
+    const int it = *a.d_it + a.step_off;
+    const int e = a.rec_elem[r];
+    const int ex = e % a.nx, ey = (e / a.nx) % a.ny, ez = e / (a.nx * a.ny);
+    const size_t nuni = (size_t)a.nuni;
+    const T *vs = a.v + (size_t)s * 3 * nuni;
+    const T *vm = a.rec_vm + (size_t)r * NP;
+    T acc[3] = {0, 0, 0};
+    for (int p = lane; p < NP; p += 32) {
+        const int i = p % P, j = (p / P) % P, k = p / (P * P);
+        const size_t u =
+            (size_t)(ex * N + i) + (size_t)a.NXU * ((size_t)(ey * N + j) + (size_t)a.NYU * (size_t)(ez * N + k));
+        const T wgt = vm[p];
+        acc[0] += wgt * vs[u];
+        acc[1] += wgt * vs[nuni + u];
+        acc[2] += wgt * vs[2 * nuni + u];
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        T x = acc[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+        acc[c] = x;
+    }
+    if (lane == 0) {
+        T *out = a.seis + (((size_t)s * a.nrec + r) * 3) * a.nt + (it - 1);
+        out[0] = acc[0];
+        out[(size_t)a.nt] = acc[1];
+        out[2 * (size_t)a.nt] = acc[2];
+    }
+}
+
+// Inverse assembled mass matrix in FP64 (src/model_paras.F90:410-415):
+// MM = -jac * r^2 * sin(theta) * rho * w_i w_j w_k summed over the copies of
+// each unique point, rho = 1/rhoinv where rhoinv > 0 else 0.
+// sin_t and r come in double from the caller's tables (dsin, dr).
+template <int N, typename T>
+__global__ void __launch_bounds__(256) k_inv_mass(const StepArgs<T> a, const T *rhoinv, const double *dsin,
+                                                  const double *dr, const double *dw, double jac) {
+    constexpr int P = N + 1, NP = P * P * P;
+    const unsigned u = blockIdx.x * 256u + threadIdx.x;
+    if (u >= (unsigned)a.nuni) return;
+    const int g[3] = {(int)(u % (unsigned)a.NXU), (int)((u / (unsigned)a.NXU) % (unsigned)a.NYU),
+                      (int)(u / ((unsigned)a.NXU * (unsigned)a.NYU))};
+    const int ne[3] = {a.nx, a.ny, a.nz};
+    int ce[3][2], cn[3][2], cnt[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const int e0 = g[d] / N, n0 = g[d] - e0 * N;
+        if (n0 == 0 && e0 > 0 && e0 < ne[d]) {
+            cnt[d] = 2;
+            ce[d][0] = e0 - 1; cn[d][0] = N;
+            ce[d][1] = e0;     cn[d][1] = 0;
+        } else {
+            cnt[d] = 1;
+            ce[d][0] = min(e0, ne[d] - 1);
+            cn[d][0] = g[d] - ce[d][0] * N;
+        }
+    }
+    double mm = 0.0;
+    for (int c2 = 0; c2 < cnt[2]; ++c2)
+        for (int c1 = 0; c1 < cnt[1]; ++c1)
+            for (int c0 = 0; c0 < cnt[0]; ++c0) {
+                const int ex = ce[0][c0], i = cn[0][c0], ey = ce[1][c1], j = cn[1][c1], ez = ce[2][c2], k = cn[2][c2];
+                const size_t e = (size_t)ex + (size_t)a.nx * (ey + (size_t)a.ny * ez);
+                const double ri = (double)rhoinv[e * NP + i + P * (j + P * k)];
+                const double rho = ri > 0.0 ? 1.0 / ri : 0.0;
+                const double rr = dr[ez * P + k];
+                mm += -(jac * rr * rr * dsin[ex * P + i] * rho * (dw[i] * dw[j] * dw[k]));
+            }
+    const_cast<T *>(a.invM)[u] = (T)(1.0 / mm);
+}
+
+template <int N, typename T>
+__global__ void __launch_bounds__(256) k_gather_local(const StepArgs<T> a, const T *uni, T *loc) {
+    constexpr int P = N + 1, NP = P * P * P;
+    const size_t li = (size_t)blockIdx.x * 256 + threadIdx.x;
+    if (li >= (size_t)a.nloc) return;
+    const size_t e = li / NP;
+    const int p = (int)(li - e * NP);
+    const int i = p % P, j = (p / P) % P, k = p / (P * P);
+    const int ex = (int)(e % a.nx), ey = (int)((e / a.nx) % a.ny), ez = (int)(e / ((size_t)a.nx * a.ny));
+    const size_t u =
+        (size_t)(ex * N + i) + (size_t)a.NXU * ((size_t)(ey * N + j) + (size_t)a.NYU * (size_t)(ez * N + k));
+    loc[li] = uni[u];
+}
+
+template <int N, typename T>
+__global__ void __launch_bounds__(256) k_scatter_unique(const StepArgs<T> a, const T *loc, T *uni) {
+    constexpr int P = N + 1, NP = P * P * P;
+    const size_t li = (size_t)blockIdx.x * 256 + threadIdx.x;
+    if (li >= (size_t)a.nloc) return;
+    const size_t e = li / NP;
+    const int p = (int)(li - e * NP);
+    const int i = p % P, j = (p / P) % P, k = p / (P * P);
+    const int ex = (int)(e % a.nx), ey = (int)((e / a.nx) % a.ny), ez = (int)(e / ((size_t)a.nx * a.ny));
+    const size_t u =
+        (size_t)(ex * N + i) + (size_t)a.NXU * ((size_t)(ey * N + j) + (size_t)a.NYU * (size_t)(ez * N + k));
+    atomicAdd(uni + u, loc[li]);
+}
+
+template <int N, typename T>
+__global__ void __launch_bounds__(256) k_taper_local(const StepArgs<T> a, T *loc) {
+    constexpr int P = N + 1, NP = P * P * P;
+    const size_t li = (size_t)blockIdx.x * 256 + threadIdx.x;
+    if (li >= (size_t)a.nloc) return;
+    const size_t e = li / NP;
+    const int p = (int)(li - e * NP);
+    const int i = p % P, j = (p / P) % P, k = p / (P * P);
+    const int ex = (int)(e % a.nx), ey = (int)((e / a.nx) % a.ny), ez = (int)(e / ((size_t)a.nx * a.ny));
+    loc[li] = taper_value(a.px[ex * P + i], a.py[ey * P + j], a.pz[ez * P + k], a.alpha);
+}
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+template <int N, typename T, int NSLS, bool ANISO>
+int launch_element_v(const StepArgs<T> &a, void *stream) {
+    using C = ElemCfg<N>;
+    const size_t smem = sizeof(T) * (4 * C::P * C::P + C::EPB * 12 * C::NP);
+    static bool attr_set = false;
+    if (!attr_set) {
+        if (cudaFuncSetAttribute(k_element<N, T, NSLS, ANISO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess)
+            return -1;
+        attr_set = true;
+    }
+    const long long blocks = (long long)((a.nel + C::EPB - 1) / C::EPB) * a.S;
+    k_element<N, T, NSLS, ANISO><<<(unsigned)blocks, C::NT, smem, (cudaStream_t)stream>>>(a);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int N, typename T>
+int launch_element(const StepArgs<T> &a, bool sls, bool aniso, void *stream) {
+    if (sls) return aniso ? launch_element_v<N, T, kNsls, true>(a, stream) : launch_element_v<N, T, kNsls, false>(a, stream);
+    return aniso ? launch_element_v<N, T, 0, true>(a, stream) : launch_element_v<N, T, 0, false>(a, stream);
+}
+
+template <int N, typename T>
+int launch_node(const StepArgs<T> &a, bool kahan, void *stream) {
+    dim3 grid((unsigned)((a.nuni + 255) / 256), (unsigned)a.S);
+    if (kahan) k_node<N, T, true><<<grid, 256, 0, (cudaStream_t)stream>>>(a);
+    else k_node<N, T, false><<<grid, 256, 0, (cudaStream_t)stream>>>(a);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int N, typename T>
+int launch_sources(const StepArgs<T> &a, void *stream) {
+    if (a.nsrc <= 0) return 0;
+    constexpr int NT = ((ElemCfg<N>::NP + 31) / 32) * 32;
+    k_sources<N, T><<<a.nsrc, NT, 0, (cudaStream_t)stream>>>(a);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int N, typename T>
+int launch_receivers(const StepArgs<T> &a, void *stream) {
+    if (a.nrec <= 0) return 0;
+    dim3 grid((unsigned)((a.nrec + 3) / 4), (unsigned)a.S);
+    k_receivers<N, T><<<grid, 128, 0, (cudaStream_t)stream>>>(a);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int N, typename T>
+int launch_gather_local(const StepArgs<T> &a, const T *uni, T *loc, void *stream) {
+    k_gather_local<N, T><<<(unsigned)((a.nloc + 255) / 256), 256, 0, (cudaStream_t)stream>>>(a, uni, loc);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int N, typename T>
+int launch_scatter_unique(const StepArgs<T> &a, const T *loc, T *uni, void *stream) {
+    k_scatter_unique<N, T><<<(unsigned)((a.nloc + 255) / 256), 256, 0, (cudaStream_t)stream>>>(a, loc, uni);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int N, typename T>
+int launch_taper_local(const StepArgs<T> &a, T *loc, void *stream) {
+    k_taper_local<N, T><<<(unsigned)((a.nloc + 255) / 256), 256, 0, (cudaStream_t)stream>>>(a, loc);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace sesnt
+
+namespace sesnt {
+
+template <int N, typename T>
+int launch_inv_mass(const StepArgs<T> &a, const T *rhoinv, const double *dsin, const double *dr, const double *dw,
+                    double jac, void *stream) {
+    k_inv_mass<N, T><<<(unsigned)((a.nuni + 255) / 256), 256, 0, (cudaStream_t)stream>>>(a, rhoinv, dsin, dr, dw,
+                                                                                         jac);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+template <int N, typename T>
+const LpdOps<T> *lpd_ops_n() {
+    static const LpdOps<T> ops = {
+        &launch_element<N, T>,        &launch_node<N, T>,        &launch_sources<N, T>,
+        &launch_receivers<N, T>,      &launch_inv_mass<N, T>,    &launch_gather_local<N, T>,
+        &launch_scatter_unique<N, T>, &launch_taper_local<N, T>, ElemCfg<N>::NT,
+        sizeof(T) * (4 * ElemCfg<N>::P * ElemCfg<N>::P + ElemCfg<N>::EPB * 12 * ElemCfg<N>::NP)};
+    return &ops;
+}
+
+}  // namespace sesnt
+
+// One translation unit per degree instantiates everything for FP32 and FP64.
+#define SESNT_INSTANTIATE_LPD(NN)                                    \
+    namespace sesnt {                                                \
+    template const LpdOps<float> *lpd_ops_n<NN, float>();            \
+    template const LpdOps<double> *lpd_ops_n<NN, double>();          \
+    }

@@ -1,0 +1,1078 @@
+// C ABI of the GB300 time step (include/sesnt.h): handle management, model
+// import and FP64 precompute, source/receiver bookkeeping, step launches
+// (direct or replayed from a captured CUDA graph), and readback in the
+// reference raw layout.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/sesnt.h"
+#include "sesnt_internal.h"
+
+using namespace sesnt;
+
+namespace sesnt {
+template <>
+const LpdOps<float> *lpd_ops<float>(int lpd) {
+    switch (lpd) {
+        case 2: return lpd_ops_n<2, float>();
+        case 3: return lpd_ops_n<3, float>();
+        case 4: return lpd_ops_n<4, float>();
+        case 5: return lpd_ops_n<5, float>();
+        case 6: return lpd_ops_n<6, float>();
+        case 7: return lpd_ops_n<7, float>();
+        default: return nullptr;
+    }
+}
+template <>
+const LpdOps<double> *lpd_ops<double>(int lpd) {
+    switch (lpd) {
+        case 2: return lpd_ops_n<2, double>();
+        case 3: return lpd_ops_n<3, double>();
+        case 4: return lpd_ops_n<4, double>();
+        case 5: return lpd_ops_n<5, double>();
+        case 6: return lpd_ops_n<6, double>();
+        case 7: return lpd_ops_n<7, double>();
+        default: return nullptr;
+    }
+}
+}  // namespace sesnt
+
+namespace {
+
+thread_local std::string g_create_error;
+
+__global__ void k_set_it(int *d_it, int v) { *d_it = v; }
+__global__ void k_advance_it(int *d_it, int by) { *d_it += by; }
+
+// out[e*NP + p] = in[p*nel + e]: reference raw layout -> element-major, via
+// 32x32 shared-memory tiles so both sides stay coalesced.
+template <typename T>
+__global__ void k_import(const float *__restrict__ in, T *__restrict__ out, int NP, long long nel) {
+    __shared__ float tile[32][33];
+    const long long e0 = (long long)blockIdx.x * 32, p0 = (long long)blockIdx.y * 32;
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        long long p = p0 + r, e = e0 + threadIdx.x;
+        if (p < NP && e < nel) tile[r][threadIdx.x] = in[p * nel + e];
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += 8) {
+        long long e = e0 + r, p = p0 + threadIdx.x;
+        if (p < NP && e < nel) out[e * NP + p] = (T)tile[threadIdx.x][r];
+    }
+}
+
+// tau = 6.0814 * q^-1.015 (src/model_paras.F90:407), evaluated in FP64.
+template <typename T>
+__global__ void k_tau(const T *q, T *tau, long long n) {
+    long long i = (long long)blockIdx.x * 256 + threadIdx.x;
+    if (i < n) tau[i] = (T)(6.0814 * pow((double)q[i], -1.015));
+}
+
+template <typename T>
+__global__ void k_minmax(const T *v, long long n, unsigned long long *mm, int *bad) {
+    // mm[0] = ordered bits of the minimum, mm[1] of the maximum (float32)
+    float lo = INFINITY, hi = -INFINITY;
+    int nonfinite = 0;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float x = (float)v[i];
+        if (!isfinite(x)) nonfinite = 1;
+        lo = fminf(lo, x);
+        hi = fmaxf(hi, x);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+        nonfinite |= __shfl_xor_sync(0xffffffffu, nonfinite, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        auto key = [](float f) -> unsigned long long {
+            unsigned b = __float_as_uint(f);
+            return (unsigned long long)((b & 0x80000000u) ? ~b : (b | 0x80000000u));
+        };
+        atomicMin(&mm[0], key(lo));
+        atomicMax(&mm[1], key(hi));
+        if (nonfinite) atomicOr(bad, 1);
+    }
+}
+
+float unkey(unsigned long long k) {
+    unsigned b = (unsigned)k;
+    b = (b & 0x80000000u) ? (b & 0x7fffffffu) : ~b;
+    float f;
+    std::memcpy(&f, &b, 4);
+    return f;
+}
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t n = 0;
+};
+
+struct HostSource {
+    int sim, elem;
+    std::vector<float> vm;
+    bool present[9];
+    std::vector<float> data[9];
+};
+
+}  // namespace
+
+struct sesnt_handle {
+    sesnt_grid_t g{};
+    int N = 0, P = 0, NP = 0, nel = 0, S = 1;
+    long long nloc = 0, nuni = 0;
+    int NXU = 0, NYU = 0, NZU = 0;
+    bool dbl = false, sls = false, aniso = false, kahan = false, use_graph = true, model_set = false;
+    int esize = 4;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    std::vector<DevBuf> bufs;
+    size_t dev_bytes = 0;
+    // device buffers (typed by precision)
+    void *tabD = nullptr, *w = nullptr, *sin_t = nullptr, *cot_t = nullptr, *r = nullptr;
+    void *px = nullptr, *py = nullptr, *pz = nullptr;
+    double *dsin = nullptr, *dr = nullptr, *dw = nullptr;
+    void *lam = nullptr, *mu = nullptr, *A = nullptr, *B = nullptr, *C = nullptr, *tau = nullptr;
+    void *sig = nullptr, *mem = nullptr, *v = nullptr, *vc = nullptr, *F = nullptr, *invM = nullptr;
+    int *d_it = nullptr;
+    double dt = 0, c1 = 0, c2 = 0, c3 = 0, jac = 0, alpha = 0;
+    // sources and receivers
+    std::vector<HostSource> sources;
+    bool src_dirty = true;
+    void *d_src = nullptr, *d_src_vm = nullptr, *d_src_data = nullptr;
+    int nsrc_rec = 0;
+    std::vector<int> rec_elem;
+    std::vector<float> rec_vm;
+    std::vector<unsigned> rec_mask;
+    bool rec_dirty = true;
+    int *d_rec_elem = nullptr;
+    void *d_rec_vm = nullptr, *d_seis = nullptr;
+    int nrec_dev = 0;
+    // graph
+    cudaGraphExec_t graph = nullptr;
+    int graph_steps = 0;
+    // events for timing
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int launches_per_step = 0;
+
+    int fail(int code, const char *fmt, ...) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        err = buf;
+        return code;
+    }
+    int cuda_fail(cudaError_t e, const char *what) {
+        return fail(SESNT_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+    }
+    int alloc(void **out, size_t bytes, const char *what) {
+        void *p = nullptr;
+        if (bytes == 0) bytes = 16;
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            return fail(SESNT_ENOMEM, "cudaMalloc of %zu bytes for %s failed: %s", bytes, what,
+                        cudaGetErrorString(e));
+        }
+        bufs.push_back({p, bytes});
+        dev_bytes += bytes;
+        *out = p;
+        return SESNT_OK;
+    }
+    void release(void *p) {
+        if (!p) return;
+        for (size_t i = 0; i < bufs.size(); ++i)
+            if (bufs[i].p == p) {
+                dev_bytes -= bufs[i].n;
+                cudaFree(p);
+                bufs.erase(bufs.begin() + i);
+                return;
+            }
+    }
+    void drop_graph() {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+        graph_steps = 0;
+    }
+    ~sesnt_handle() {
+        drop_graph();
+        if (stream) cudaStreamSynchronize(stream);
+        for (auto &b : bufs) cudaFree(b.p);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+        if (stream) cudaStreamDestroy(stream);
+    }
+
+    template <typename T>
+    StepArgs<T> args() const {
+        StepArgs<T> a{};
+        a.nx = g.nx; a.ny = g.ny; a.nz = g.nz; a.nel = nel; a.S = S;
+        a.NXU = NXU; a.NYU = NYU; a.NZU = NZU; a.nuni = nuni; a.nloc = nloc;
+        a.dt = (T)dt; a.c1 = (T)c1; a.c2 = (T)c2; a.c3 = (T)c3; a.jac = (T)jac; a.alpha = (T)alpha;
+        for (int q = 0; q < kNsls; ++q) a.tau_p[q] = (T)kTauP[q];
+        a.tabD = (const T *)tabD; a.w = (const T *)w; a.sin_t = (const T *)sin_t; a.cot_t = (const T *)cot_t;
+        a.r = (const T *)r; a.px = (const T *)px; a.py = (const T *)py; a.pz = (const T *)pz;
+        a.lam = (const T *)lam; a.mu = (const T *)mu; a.A = (const T *)A; a.B = (const T *)B; a.C = (const T *)C;
+        a.tau = (const T *)tau;
+        a.sig = (T *)sig; a.mem = (T *)mem; a.v = (T *)v; a.vc = (T *)vc; a.F = (T *)F; a.invM = (const T *)invM;
+        a.nsrc = nsrc_rec; a.nt = g.nt; a.src = (const SrcRec *)d_src; a.src_vm = (const T *)d_src_vm;
+        a.src_data = (const T *)d_src_data;
+        a.nrec = nrec_dev; a.rec_elem = d_rec_elem; a.rec_vm = (const T *)d_rec_vm; a.seis = (T *)d_seis;
+        a.d_it = d_it; a.step_off = 0;
+        return a;
+    }
+};
+
+namespace {
+
+int check_grid(const sesnt_grid_t *g, std::string &why) {
+    char b[256];
+    auto bad = [&](const char *m) { why = m; return SESNT_EINVAL; };
+    if (!g) return bad("grid is NULL");
+    // src/config/config.F90:106-115, 168-179, 214-217
+    if (g->nx < 4 || g->ny < 4 || g->nz < 4) return bad("nx, ny and nz must be at least 4");
+    if (g->lpd < kMinLpd || g->lpd > kMaxLpd) {
+        snprintf(b, sizeof b, "lpd=%d not supported (this library is built for lpd %d..%d)", g->lpd, kMinLpd,
+                 kMaxLpd);
+        why = b;
+        return SESNT_EUNSUPPORTED;
+    }
+    if (g->taper_width < 0 || 2 * g->taper_width + 1 > std::min(g->nx, std::min(g->ny, g->nz)))
+        return bad("taper_width too wide (2*taper_width+1 must not exceed nx, ny, nz)");
+    if (!(g->lat_min <= g->lat_max) || !(g->lon_min <= g->lon_max) || !(g->rad_min <= g->rad_max))
+        return bad("domain bounds out of order");
+    if (!(std::fabs(g->lat_min) <= 90.f && std::fabs(g->lat_max) <= 90.f)) return bad("invalid latitude");
+    if (!(std::fabs(g->lon_min) <= 180.f && std::fabs(g->lon_max) <= 180.f)) return bad("invalid longitude");
+    if (!(g->rad_min >= 1.0f && g->rad_max >= 1.0f)) return bad("invalid radius");
+    if (g->nt < 2 || g->nt > 50000) return bad("nt must be in [2, 50000]");
+    if (!(g->dt > 0.0f)) return bad("dt must be positive");
+    if (g->taper_width > 0 && !(g->taper_slope > 0.0f)) return bad("taper_slope must be positive");
+    if (g->n_sls != 0 && g->n_sls != kNsls) return bad("n_sls must be 0 or 3");
+    if (g->precision != 4 && g->precision != 8) return bad("precision must be 4 (FP32) or 8 (FP64)");
+    if (g->batch < 1) return bad("batch must be >= 1");
+    const long long P = g->lpd + 1;
+    const long long nuni = (g->nx * (long long)g->lpd + 1) * (g->ny * (long long)g->lpd + 1) *
+                           (g->nz * (long long)g->lpd + 1);
+    const long long nloc = (long long)g->nx * g->ny * g->nz * P * P * P;
+    if (nuni >= (1LL << 31) || nloc >= (1LL << 40)) return bad("grid too large for 32-bit unique indices");
+    return SESNT_OK;
+}
+
+template <typename T>
+int upload(sesnt_t *h, void *dst, const std::vector<T> &src, const char *what) {
+    cudaError_t e = cudaMemcpy(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice);
+    return e == cudaSuccess ? SESNT_OK : h->cuda_fail(e, what);
+}
+
+template <typename T>
+int setup_tables(sesnt_t *h) {
+    const sesnt_grid_t &g = h->g;
+    const int N = g.lpd, P = N + 1;
+    Domain<T> d = make_domain<T>(g.nx, g.ny, g.nz, g.lat_min, g.lat_max, g.lon_min, g.lon_max, g.rad_min, g.rad_max);
+    // FP64 derived quantities from the working-precision domain
+    const double dx = (double)d.dx_elm, dy = (double)d.dy_elm, dz = (double)d.dz_elm;
+    h->jac = dx * dy * dz / 8.0;                // src/geometric_paras.f90:129
+    h->c1 = (2.0 / dx) * h->jac;                // src/evolution.f90:337-339
+    h->c2 = (2.0 / dy) * h->jac;
+    h->c3 = -((2.0 / dz) * h->jac);
+    h->dt = (double)(T)g.dt;
+    h->alpha = (double)(T)g.taper_slope;
+    std::vector<double> dl = lagrange_derivative_matrix<double>(N);
+    std::vector<T> tab(4 * P * P);
+    for (int q = 0; q < P; ++q)
+        for (int i = 0; i < P; ++i) {
+            tab[0 * P * P + q * P + i] = (T)(2.0 * dl[q * P + i] / dx);  // strain, :133-135
+            tab[1 * P * P + q * P + i] = (T)(2.0 * dl[q * P + i] / dy);
+            tab[2 * P * P + q * P + i] = (T)(2.0 * dl[q * P + i] / dz);
+            tab[3 * P * P + i * P + q] = (T)dl[i * P + q];  // divergence, :344-346
+        }
+    std::vector<double> wd = gll_quadrature_weights<double>(N);
+    std::vector<T> wt(P);
+    for (int i = 0; i < P; ++i) wt[i] = (T)wd[i];
+    std::vector<T> xc = element_coordinates<T>(g.nx, N, d.x_loc_min, d.x_loc_max);
+    std::vector<T> zc = element_coordinates<T>(g.nz, N, d.z_loc_max, d.z_loc_min);  // radius decreases with k
+    std::vector<T> st(xc.size()), ct(xc.size()), rr(zc.size());
+    std::vector<double> dsin(xc.size()), drr(zc.size());
+    for (size_t a = 0; a < xc.size(); ++a) {
+        const double th = (double)xc[a];
+        dsin[a] = std::sin(th);
+        st[a] = (T)dsin[a];
+        ct[a] = (T)(std::cos(th) / std::sin(th));
+    }
+    for (size_t a = 0; a < zc.size(); ++a) {
+        drr[a] = (double)zc[a];
+        rr[a] = zc[a];
+    }
+    std::vector<T> pxv, pyv, pzv;
+    taper_profiles<T>(g.nx, g.ny, g.nz, N, g.taper_width, (T)g.taper_slope, d, pxv, pyv, pzv);
+    int rc;
+    if ((rc = upload(h, h->tabD, tab, "tables"))) return rc;
+    if ((rc = upload(h, h->w, wt, "weights"))) return rc;
+    if ((rc = upload(h, h->sin_t, st, "sin"))) return rc;
+    if ((rc = upload(h, h->cot_t, ct, "cot"))) return rc;
+    if ((rc = upload(h, h->r, rr, "r"))) return rc;
+    if ((rc = upload(h, h->px, pxv, "px"))) return rc;
+    if ((rc = upload(h, h->py, pyv, "py"))) return rc;
+    if ((rc = upload(h, h->pz, pzv, "pz"))) return rc;
+    if ((rc = upload(h, h->dsin, dsin, "dsin"))) return rc;
+    if ((rc = upload(h, h->dr, drr, "dr"))) return rc;
+    if ((rc = upload(h, h->dw, wd, "dw"))) return rc;
+    return SESNT_OK;
+}
+
+template <typename T>
+const LpdOps<T> *ops(const sesnt_t *h) {
+    return lpd_ops<T>(h->N);
+}
+
+int zero_state(sesnt_t *h) {
+    const size_t E = h->esize;
+    struct Z { void *p; size_t n; } zs[] = {
+        {h->sig, E * 6 * (size_t)h->nloc * h->S},
+        {h->mem, h->sls ? E * 6 * kNsls * (size_t)h->nloc * h->S : 0},
+        {h->v, E * 3 * (size_t)h->nuni * h->S},
+        {h->vc, h->kahan ? E * 3 * (size_t)h->nuni * h->S : 0},
+        {h->F, E * 3 * (size_t)h->nuni * h->S},
+        {h->d_seis, E * (size_t)h->S * h->rec_elem.size() * 3 * h->g.nt}};
+    for (auto &z : zs)
+        if (z.p && z.n) {
+            cudaError_t e = cudaMemsetAsync(z.p, 0, z.n, h->stream);
+            if (e != cudaSuccess) return h->cuda_fail(e, "zeroing state");
+        }
+    return SESNT_OK;
+}
+
+// Resolve sources per (simulation, element): for each component the last
+// registered source defining it wins (the reference assigns element slabs,
+// src/config/channel_mod.f90:866-867), then upload.
+template <typename T>
+int upload_sources(sesnt_t *h) {
+    h->release(h->d_src); h->release(h->d_src_vm); h->release(h->d_src_data);
+    h->d_src = h->d_src_vm = h->d_src_data = nullptr;
+    h->nsrc_rec = 0;
+    h->src_dirty = false;
+    if (h->sources.empty()) return SESNT_OK;
+    std::vector<SrcRec> recs;
+    std::vector<T> vm, data;
+    int nvm = 0, ndata = 0;
+    std::vector<std::vector<int>> data_row(h->sources.size(), std::vector<int>(9, -1));
+    for (size_t s = 0; s < h->sources.size(); ++s) {
+        const HostSource &hs = h->sources[s];
+        for (float x : hs.vm) vm.push_back((T)x);
+        for (int c = 0; c < 9; ++c)
+            if (hs.present[c]) {
+                for (float x : hs.data[c]) data.push_back((T)x);
+                data_row[s][c] = ndata++;
+            }
+        ++nvm;
+    }
+    for (size_t s = 0; s < h->sources.size(); ++s) {
+        const HostSource &hs = h->sources[s];
+        SrcRec *r = nullptr;
+        for (auto &x : recs)
+            if (x.sim == hs.sim && x.elem == hs.elem) r = &x;
+        if (!r) {
+            SrcRec nr{};
+            nr.sim = hs.sim;
+            nr.elem = hs.elem;
+            for (int c = 0; c < 9; ++c) nr.vm[c] = nr.data[c] = -1;
+            recs.push_back(nr);
+            r = &recs.back();
+        }
+        for (int c = 0; c < 9; ++c)
+            if (hs.present[c]) {
+                r->vm[c] = (int)s;
+                r->data[c] = data_row[s][c];
+            }
+    }
+    (void)nvm;
+    int rc;
+    if ((rc = h->alloc(&h->d_src, recs.size() * sizeof(SrcRec), "source records"))) return rc;
+    if ((rc = h->alloc(&h->d_src_vm, vm.size() * sizeof(T), "source weights"))) return rc;
+    if ((rc = h->alloc(&h->d_src_data, std::max<size_t>(1, data.size()) * sizeof(T), "source data"))) return rc;
+    cudaError_t e = cudaMemcpy(h->d_src, recs.data(), recs.size() * sizeof(SrcRec), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_src_vm, vm.data(), vm.size() * sizeof(T), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !data.empty())
+        e = cudaMemcpy(h->d_src_data, data.data(), data.size() * sizeof(T), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return h->cuda_fail(e, "uploading sources");
+    h->nsrc_rec = (int)recs.size();
+    return SESNT_OK;
+}
+
+template <typename T>
+int upload_receivers(sesnt_t *h) {
+    h->rec_dirty = false;
+    const size_t nrec = h->rec_elem.size();
+    if (nrec == (size_t)h->nrec_dev && h->d_seis) return SESNT_OK;
+    // keep already recorded samples of existing receivers
+    std::vector<T> old;
+    const size_t per = (size_t)3 * h->g.nt;
+    if (h->d_seis && h->nrec_dev > 0) {
+        old.resize((size_t)h->S * h->nrec_dev * per);
+        cudaError_t e = cudaMemcpy(old.data(), h->d_seis, old.size() * sizeof(T), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return h->cuda_fail(e, "reading seismograms");
+    }
+    h->release(h->d_rec_elem); h->release(h->d_rec_vm); h->release(h->d_seis);
+    h->d_rec_elem = nullptr; h->d_rec_vm = h->d_seis = nullptr;
+    h->nrec_dev = 0;
+    if (nrec == 0) return SESNT_OK;
+    int rc;
+    if ((rc = h->alloc((void **)&h->d_rec_elem, nrec * sizeof(int), "receiver elements"))) return rc;
+    if ((rc = h->alloc(&h->d_rec_vm, nrec * h->NP * sizeof(T), "receiver weights"))) return rc;
+    if ((rc = h->alloc(&h->d_seis, (size_t)h->S * nrec * per * sizeof(T), "seismograms"))) return rc;
+    std::vector<T> vm(h->rec_vm.begin(), h->rec_vm.end());
+    std::vector<T> seis((size_t)h->S * nrec * per, T(0));
+    if (!old.empty()) {
+        const size_t oldn = old.size() / ((size_t)h->S * per);
+        for (int s = 0; s < h->S; ++s)
+            std::copy(old.begin() + (size_t)s * oldn * per, old.begin() + (size_t)(s + 1) * oldn * per,
+                      seis.begin() + (size_t)s * nrec * per);
+    }
+    cudaError_t e = cudaMemcpy(h->d_rec_elem, h->rec_elem.data(), nrec * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_rec_vm, vm.data(), vm.size() * sizeof(T), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_seis, seis.data(), seis.size() * sizeof(T), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return h->cuda_fail(e, "uploading receivers");
+    h->nrec_dev = (int)nrec;
+    return SESNT_OK;
+}
+
+template <typename T>
+int prepare_run(sesnt_t *h) {
+    if (!h->model_set) return h->fail(SESNT_ESTATE, "sesnt_set_model must be called before stepping");
+    int rc;
+    if (h->src_dirty) {
+        h->drop_graph();
+        if ((rc = upload_sources<T>(h))) return rc;
+    }
+    if (h->rec_dirty) {
+        h->drop_graph();
+        if ((rc = upload_receivers<T>(h))) return rc;
+    }
+    return SESNT_OK;
+}
+
+// Enqueue steps [it, it+n) given that *d_it == it: element, sources, node,
+// receivers per step.
+template <typename T>
+int enqueue_steps(sesnt_t *h, int n) {
+    const LpdOps<T> *o = ops<T>(h);
+    StepArgs<T> a = h->args<T>();
+    for (int q = 0; q < n; ++q) {
+        a.step_off = q;
+        if (o->element(a, h->sls, h->aniso, h->stream)) return h->fail(SESNT_ECUDA, "element kernel launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+        if (o->sources(a, h->stream)) return h->fail(SESNT_ECUDA, "source kernel launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+        if (o->node(a, h->kahan, h->stream)) return h->fail(SESNT_ECUDA, "node kernel launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+        if (o->receivers(a, h->stream)) return h->fail(SESNT_ECUDA, "receiver kernel launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+    }
+    return SESNT_OK;
+}
+
+constexpr int kGraphSteps = 32;
+
+template <typename T>
+int build_graph(sesnt_t *h) {
+    h->drop_graph();
+    cudaGraph_t gr = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return h->cuda_fail(e, "cudaStreamBeginCapture");
+    int rc = enqueue_steps<T>(h, kGraphSteps);
+    if (!rc) k_advance_it<<<1, 1, 0, h->stream>>>(h->d_it, kGraphSteps);
+    e = cudaStreamEndCapture(h->stream, &gr);
+    if (rc) {
+        if (gr) cudaGraphDestroy(gr);
+        return rc;
+    }
+    if (e != cudaSuccess) return h->cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&h->graph, gr, 0);
+    cudaGraphDestroy(gr);
+    if (e != cudaSuccess) {
+        h->graph = nullptr;
+        return h->cuda_fail(e, "cudaGraphInstantiate");
+    }
+    h->graph_steps = kGraphSteps;
+    return SESNT_OK;
+}
+
+template <typename T>
+int run_impl(sesnt_t *h, int it0, int nsteps) {
+    if (nsteps <= 0) return SESNT_OK;
+    if (it0 < 1 || it0 + nsteps - 1 > h->g.nt)
+        return h->fail(SESNT_ERANGE, "steps %d..%d outside 1..nt=%d", it0, it0 + nsteps - 1, h->g.nt);
+    int rc;
+    if ((rc = prepare_run<T>(h))) return rc;
+    k_set_it<<<1, 1, 0, h->stream>>>(h->d_it, it0);
+    int left = nsteps;
+    if (h->use_graph && nsteps >= kGraphSteps) {
+        if (!h->graph && (rc = build_graph<T>(h))) return rc;
+        while (left >= kGraphSteps) {
+            cudaError_t e = cudaGraphLaunch(h->graph, h->stream);
+            if (e != cudaSuccess) return h->cuda_fail(e, "cudaGraphLaunch");
+            left -= kGraphSteps;
+        }
+    }
+    if (left > 0 && (rc = enqueue_steps<T>(h, left))) return rc;
+    return SESNT_OK;
+}
+
+int run_any(sesnt_t *h, int it0, int nsteps) {
+    return h->dbl ? run_impl<double>(h, it0, nsteps) : run_impl<float>(h, it0, nsteps);
+}
+
+// Element-major [e][p] -> reference raw layout [p][e], with conversion.
+template <typename TI, typename TO>
+void export_layout(const TI *in, TO *out, long long nel, int NP) {
+    for (long long e = 0; e < nel; ++e)
+        for (int p = 0; p < NP; ++p) out[(size_t)p * nel + e] = (TO)in[(size_t)e * NP + p];
+}
+
+template <typename T>
+int get_field_impl(sesnt_t *h, int sim, int which, void *out, int out_prec) {
+    const LpdOps<T> *o = ops<T>(h);
+    StepArgs<T> a = h->args<T>();
+    const size_t nloc = (size_t)h->nloc, nuni = (size_t)h->nuni;
+    void *scratch = nullptr;
+    int rc;
+    if ((rc = h->alloc(&scratch, nloc * sizeof(T), "field scratch"))) return rc;
+    T *loc = (T *)scratch;
+    const T *src = nullptr;
+    bool inverse = false;
+    if (which >= 0 && which <= 2) {
+        rc = o->gather_local(a, (const T *)h->v + ((size_t)sim * 3 + which) * nuni, loc, h->stream);
+    } else if (which >= 3 && which <= 8) {
+        src = (const T *)h->sig + ((size_t)sim * 6 + (which - 3)) * nloc;
+    } else if (which == SESNT_FIELD_TAPER) {
+        rc = o->taper_local(a, loc, h->stream);
+    } else if (which == SESNT_FIELD_MASS) {
+        rc = o->gather_local(a, (const T *)h->invM, loc, h->stream);
+        inverse = true;
+    } else if (which >= SESNT_FIELD_MEMORY && which < SESNT_FIELD_MEMORY + 6 * kNsls && h->sls) {
+        const int c = (which - SESNT_FIELD_MEMORY) / kNsls, q = (which - SESNT_FIELD_MEMORY) % kNsls;
+        src = (const T *)h->mem + ((size_t)sim * 6 * kNsls + c * kNsls + q) * nloc;
+    } else {
+        h->release(scratch);
+        return h->fail(SESNT_EINVAL, "unknown or unavailable field %d", which);
+    }
+    if (rc) {
+        h->release(scratch);
+        return h->fail(SESNT_ECUDA, "field kernel failed");
+    }
+    std::vector<T> host(nloc);
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(host.data(), src ? src : loc, nloc * sizeof(T), cudaMemcpyDeviceToHost);
+    h->release(scratch);
+    if (e != cudaSuccess) return h->cuda_fail(e, "reading field");
+    if (inverse)
+        for (auto &x : host) x = T(1) / x;
+    if (out_prec == 8) export_layout(host.data(), (double *)out, h->nel, h->NP);
+    else export_layout(host.data(), (float *)out, h->nel, h->NP);
+    return SESNT_OK;
+}
+
+template <typename T>
+int set_model_impl(sesnt_t *h, const float *rhoinv, const float *lambda, const float *mu, const float *a,
+                   const float *b, const float *c, const float *q) {
+    const size_t nloc = (size_t)h->nloc;
+    // attenuation and anisotropy switches (src/evolution.f90:64-74)
+    bool has_q = false;
+    if (q)
+        for (size_t i = 0; i < nloc; ++i)
+            if (q[i] != std::numeric_limits<float>::max()) { has_q = true; break; }
+    if (has_q && !h->sls)
+        return h->fail(SESNT_EINVAL, "model has attenuation (q) but the handle was created with n_sls=0");
+    if (h->sls && !has_q) return h->fail(SESNT_EINVAL, "n_sls=3 needs a q model");
+    for (size_t i = 0; i < nloc; ++i)
+        if (!(rhoinv[i] > 0.0f) || !std::isfinite(rhoinv[i]) || !std::isfinite(lambda[i]) || !std::isfinite(mu[i]))
+            return h->fail(SESNT_EINVAL, "rhoinv must be positive and lambda, mu finite (first bad point %zu)", i);
+    bool aniso = false;
+    for (const float *x : {a, b, c})
+        if (x)
+            for (size_t i = 0; i < nloc && !aniso; ++i)
+                if (x[i] != 0.0f) aniso = true;
+    h->drop_graph();
+    // (re)allocate the optional model arrays
+    int rc;
+    if (aniso && !h->A) {
+        if ((rc = h->alloc(&h->A, nloc * sizeof(T), "A"))) return rc;
+        if ((rc = h->alloc(&h->B, nloc * sizeof(T), "B"))) return rc;
+        if ((rc = h->alloc(&h->C, nloc * sizeof(T), "C"))) return rc;
+    }
+    h->aniso = aniso;
+    void *stage = nullptr, *rho_loc = nullptr;
+    if ((rc = h->alloc(&stage, nloc * sizeof(float), "model staging"))) return rc;
+    if ((rc = h->alloc(&rho_loc, nloc * sizeof(T), "rhoinv"))) { h->release(stage); return rc; }
+    dim3 tb(32, 8), tg((unsigned)((h->nel + 31) / 32), (unsigned)((h->NP + 31) / 32));
+    auto import = [&](const float *src, void *dst) -> int {
+        cudaError_t e = cudaMemcpy(stage, src, nloc * sizeof(float), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return h->cuda_fail(e, "copying model");
+        k_import<T><<<tg, tb, 0, h->stream>>>((const float *)stage, (T *)dst, h->NP, h->nel);
+        e = cudaStreamSynchronize(h->stream);
+        return e == cudaSuccess ? SESNT_OK : h->cuda_fail(e, "importing model");
+    };
+    rc = import(rhoinv, rho_loc);
+    if (!rc) rc = import(lambda, h->lam);
+    if (!rc) rc = import(mu, h->mu);
+    if (!rc && aniso) {
+        auto imp_or_zero = [&](const float *x, void *dst) -> int {
+            if (x) return import(x, dst);
+            cudaError_t e = cudaMemset(dst, 0, nloc * sizeof(T));
+            return e == cudaSuccess ? SESNT_OK : h->cuda_fail(e, "zeroing anisotropy");
+        };
+        rc = imp_or_zero(a, h->A);
+        if (!rc) rc = imp_or_zero(b, h->B);
+        if (!rc) rc = imp_or_zero(c, h->C);
+    }
+    if (!rc && h->sls) {
+        rc = import(q, h->tau);  // q imported in place, then mapped to tau
+        if (!rc) {
+            k_tau<T><<<(unsigned)((nloc + 255) / 256), 256, 0, h->stream>>>((const T *)h->tau, (T *)h->tau,
+                                                                            (long long)nloc);
+        }
+    }
+    if (!rc) {
+        StepArgs<T> sa = h->args<T>();
+        if (ops<T>(h)->inv_mass(sa, (const T *)rho_loc, h->dsin, h->dr, h->dw, h->jac, h->stream))
+            rc = h->fail(SESNT_ECUDA, "inverse mass kernel failed");
+    }
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    h->release(stage);
+    h->release(rho_loc);
+    if (rc) return rc;
+    if (e != cudaSuccess) return h->cuda_fail(e, "model precompute");
+    h->model_set = true;
+    if ((rc = zero_state(h))) return rc;
+    e = cudaStreamSynchronize(h->stream);
+    return e == cudaSuccess ? SESNT_OK : h->cuda_fail(e, "zeroing state");
+}
+
+template <typename T>
+int get_seis_impl(sesnt_t *h, float *out) {
+    const size_t nrec = h->rec_elem.size(), per = (size_t)3 * h->g.nt;
+    if (nrec == 0) return SESNT_OK;
+    int rc;
+    if (h->rec_dirty && (rc = upload_receivers<T>(h))) return rc;
+    std::vector<T> host((size_t)h->S * nrec * per);
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(host.data(), h->d_seis, host.size() * sizeof(T), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return h->cuda_fail(e, "reading seismograms");
+    for (int s = 0; s < h->S; ++s)
+        for (size_t r = 0; r < nrec; ++r)
+            for (int c = 0; c < 3; ++c) {
+                const bool on = (h->rec_mask[r] >> c) & 1u;
+                const size_t base = (((size_t)s * nrec + r) * 3 + c) * h->g.nt;
+                for (int t = 0; t < h->g.nt; ++t) out[base + t] = on ? (float)host[base + t] : 0.0f;
+            }
+    return SESNT_OK;
+}
+
+template <typename T>
+int v_ptp_impl(sesnt_t *h, int sim, float out[2]) {
+    unsigned long long *mm = nullptr;
+    int rc;
+    if ((rc = h->alloc((void **)&mm, 2 * sizeof(unsigned long long) + sizeof(int), "ptp"))) return rc;
+    unsigned long long init[2] = {~0ULL, 0ULL};
+    int zero = 0;
+    cudaError_t e = cudaMemcpy(mm, init, sizeof init, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(mm + 2, &zero, sizeof zero, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        k_minmax<T><<<4 * 152, 256, 0, h->stream>>>((const T *)h->v + (size_t)sim * 3 * h->nuni,
+                                                    3 * h->nuni, mm, (int *)(mm + 2));
+        e = cudaStreamSynchronize(h->stream);
+    }
+    unsigned long long res[2];
+    int bad = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(res, mm, sizeof res, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&bad, mm + 2, sizeof bad, cudaMemcpyDeviceToHost);
+    h->release(mm);
+    if (e != cudaSuccess) return h->cuda_fail(e, "v_ptp");
+    out[0] = unkey(res[0]);
+    out[1] = unkey(res[1]);
+    if (bad) return h->fail(SESNT_ENONFINITE, "wavefield of simulation %d contains NaN or Inf", sim);
+    return SESNT_OK;
+}
+
+template <typename T>
+int assemble_impl(sesnt_t *h, float *field) {
+    const size_t nloc = (size_t)h->nloc, nuni = (size_t)h->nuni;
+    void *loc = nullptr, *uni = nullptr, *stage = nullptr;
+    int rc;
+    if ((rc = h->alloc(&stage, nloc * sizeof(float), "assemble staging"))) return rc;
+    if ((rc = h->alloc(&loc, nloc * sizeof(T), "assemble local"))) { h->release(stage); return rc; }
+    if ((rc = h->alloc(&uni, nuni * sizeof(T), "assemble unique"))) { h->release(stage); h->release(loc); return rc; }
+    dim3 tb(32, 8), tg((unsigned)((h->nel + 31) / 32), (unsigned)((h->NP + 31) / 32));
+    cudaError_t e = cudaMemcpy(stage, field, nloc * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemsetAsync(uni, 0, nuni * sizeof(T), h->stream);
+    StepArgs<T> a = h->args<T>();
+    if (e == cudaSuccess) {
+        k_import<T><<<tg, tb, 0, h->stream>>>((const float *)stage, (T *)loc, h->NP, h->nel);
+        if (ops<T>(h)->scatter_unique(a, (const T *)loc, (T *)uni, h->stream) ||
+            ops<T>(h)->gather_local(a, (const T *)uni, (T *)loc, h->stream))
+            e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    }
+    std::vector<T> host(nloc);
+    if (e == cudaSuccess) e = cudaMemcpy(host.data(), loc, nloc * sizeof(T), cudaMemcpyDeviceToHost);
+    h->release(stage); h->release(loc); h->release(uni);
+    if (e != cudaSuccess) return h->cuda_fail(e, "assemble_field");
+    export_layout(host.data(), field, h->nel, h->NP);
+    return SESNT_OK;
+}
+
+size_t footprint(const sesnt_grid_t *g, bool aniso) {
+    const size_t P = g->lpd + 1, NP = P * P * P;
+    const size_t nel = (size_t)g->nx * g->ny * g->nz, nloc = nel * NP;
+    const size_t nuni = ((size_t)g->nx * g->lpd + 1) * ((size_t)g->ny * g->lpd + 1) * ((size_t)g->nz * g->lpd + 1);
+    const size_t E = g->precision == 8 ? 8 : 4, S = g->batch;
+    size_t b = 0;
+    b += nloc * E * (2 + (aniso ? 3 : 0) + (g->n_sls ? 1 : 0));    // lambda, mu, A,B,C, tau
+    b += nloc * E * S * (6 + (g->n_sls ? 6 * kNsls : 0));          // sigma, memory
+    b += nuni * E * (1 + S * (6 + ((g->flags & SESNT_FLAG_KAHAN) ? 3 : 0)));  // invM, v, F, comp
+    b += nloc * (sizeof(float) + E);                                // set_model staging + rhoinv (transient)
+    b += 1 << 20;                                                   // tables, counters
+    return b;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sesnt_create(const sesnt_grid_t *grid, sesnt_t **out) {
+    if (!out) {
+        g_create_error = "out is NULL";
+        return SESNT_EINVAL;
+    }
+    *out = nullptr;
+    std::string why;
+    int rc = check_grid(grid, why);
+    if (rc) {
+        g_create_error = why;
+        return rc;
+    }
+    std::unique_ptr<sesnt_handle> h(new sesnt_handle());
+    h->g = *grid;
+    h->N = grid->lpd;
+    h->P = h->N + 1;
+    h->NP = h->P * h->P * h->P;
+    h->nel = grid->nx * grid->ny * grid->nz;
+    h->nloc = (long long)h->nel * h->NP;
+    h->NXU = grid->nx * h->N + 1;
+    h->NYU = grid->ny * h->N + 1;
+    h->NZU = grid->nz * h->N + 1;
+    h->nuni = (long long)h->NXU * h->NYU * h->NZU;
+    h->S = grid->batch;
+    h->dbl = grid->precision == 8;
+    h->esize = h->dbl ? 8 : 4;
+    h->sls = grid->n_sls > 0;
+    h->kahan = (grid->flags & SESNT_FLAG_KAHAN) != 0;
+    h->use_graph = (grid->flags & SESNT_FLAG_NO_GRAPH) == 0;
+    h->launches_per_step = 4;
+    cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        g_create_error = std::string("cudaStreamCreate: ") + cudaGetErrorString(e);
+        return SESNT_ECUDA;
+    }
+    cudaEventCreate(&h->ev0);
+    cudaEventCreate(&h->ev1);
+    const size_t E = h->esize, P = h->P, nloc = (size_t)h->nloc, nuni = (size_t)h->nuni, S = h->S;
+    struct A { void **p; size_t n; const char *w; } allocs[] = {
+        {&h->tabD, 4 * P * P * E, "tables"}, {&h->w, P * E, "weights"},
+        {&h->sin_t, grid->nx * P * E, "sin"}, {&h->cot_t, grid->nx * P * E, "cot"},
+        {&h->r, grid->nz * P * E, "r"}, {&h->px, grid->nx * P * E, "px"},
+        {&h->py, grid->ny * P * E, "py"}, {&h->pz, grid->nz * P * E, "pz"},
+        {(void **)&h->dsin, grid->nx * P * 8, "dsin"}, {(void **)&h->dr, grid->nz * P * 8, "dr"},
+        {(void **)&h->dw, P * 8, "dw"},
+        {&h->lam, nloc * E, "lambda"}, {&h->mu, nloc * E, "mu"},
+        {&h->sig, 6 * nloc * E * S, "stress"},
+        {&h->v, 3 * nuni * E * S, "velocity"}, {&h->F, 3 * nuni * E * S, "force"},
+        {&h->invM, nuni * E, "inverse mass"}, {(void **)&h->d_it, sizeof(int), "step counter"}};
+    for (auto &a : allocs)
+        if ((rc = h->alloc(a.p, a.n, a.w))) {
+            g_create_error = h->err;
+            return rc;
+        }
+    if (h->sls) {
+        if ((rc = h->alloc(&h->tau, nloc * E, "tau")) || (rc = h->alloc(&h->mem, 6 * kNsls * nloc * E * S, "memory"))) {
+            g_create_error = h->err;
+            return rc;
+        }
+    }
+    if (h->kahan && (rc = h->alloc(&h->vc, 3 * nuni * E * S, "compensation"))) {
+        g_create_error = h->err;
+        return rc;
+    }
+    rc = h->dbl ? setup_tables<double>(h.get()) : setup_tables<float>(h.get());
+    if (rc) {
+        g_create_error = h->err;
+        return rc;
+    }
+    if ((rc = zero_state(h.get()))) {
+        g_create_error = h->err;
+        return rc;
+    }
+    *out = h.release();
+    return SESNT_OK;
+}
+
+int sesnt_destroy(sesnt_t *h) {
+    delete h;
+    return SESNT_OK;
+}
+
+const char *sesnt_last_error(const sesnt_t *h) {
+    if (!h) return g_create_error.c_str();
+    return h->err.c_str();
+}
+
+int sesnt_set_model(sesnt_t *h, const float *rhoinv, const float *lambda, const float *mu, const float *a,
+                    const float *b, const float *c, const float *q) {
+    if (!h) return SESNT_EINVAL;
+    if (!rhoinv || !lambda || !mu) return h->fail(SESNT_EINVAL, "rhoinv, lambda and mu are required");
+    return h->dbl ? set_model_impl<double>(h, rhoinv, lambda, mu, a, b, c, q)
+                  : set_model_impl<float>(h, rhoinv, lambda, mu, a, b, c, q);
+}
+
+int sesnt_locate_point(const sesnt_grid_t *grid, float lat, float lon, float depth, int elem[3], float *vanderm) {
+    if (!grid || !elem || !vanderm) {
+        g_create_error = "grid, elem and vanderm are required";
+        return SESNT_EINVAL;
+    }
+    std::string why;
+    if (grid->lpd < kMinLpd || grid->lpd > kMaxLpd || grid->nx < 1 || grid->ny < 1 || grid->nz < 1) {
+        g_create_error = "invalid grid";
+        return SESNT_EINVAL;
+    }
+    int rc = locate_point(grid->nx, grid->ny, grid->nz, grid->lpd, grid->lat_min, grid->lat_max, grid->lon_min,
+                          grid->lon_max, grid->rad_min, grid->rad_max, lat, lon, depth, elem, vanderm, why);
+    if (rc) {
+        char b[256];
+        snprintf(b, sizeof b, "%s (lat=%g lon=%g depth=%g)", why.c_str(), (double)lat, (double)lon, (double)depth);
+        g_create_error = b;
+        return rc == -1 ? SESNT_EINVAL : SESNT_ENOTFOUND;
+    }
+    return SESNT_OK;
+}
+
+int sesnt_source_signature(int wavelet, float onset, float width, float dt, int nt, float *out) {
+    if (!out || nt < 1) return SESNT_EINVAL;
+    return source_signature(wavelet, onset, width, dt, nt, out) ? SESNT_EINVAL : SESNT_OK;
+}
+
+int sesnt_add_source(sesnt_t *h, int sim, int ex, int ey, int ez, const float *vanderm, int kind, const float *comp,
+                     const float *stf, int nt) {
+    if (!h) return SESNT_EINVAL;
+    if (!vanderm || !comp || !stf) return h->fail(SESNT_EINVAL, "vanderm, comp and stf are required");
+    if (sim < 0 || sim >= h->S) return h->fail(SESNT_ERANGE, "simulation %d outside 0..%d", sim, h->S - 1);
+    if (ex < 0 || ex >= h->g.nx || ey < 0 || ey >= h->g.ny || ez < 0 || ez >= h->g.nz)
+        return h->fail(SESNT_ERANGE, "element (%d,%d,%d) outside the grid", ex, ey, ez);
+    if (nt != h->g.nt) return h->fail(SESNT_EINVAL, "stf has %d samples, nt=%d", nt, h->g.nt);
+    if (kind != SESNT_SOURCE_MT && kind != SESNT_SOURCE_SF) return h->fail(SESNT_EINVAL, "unknown source kind %d", kind);
+    HostSource s;
+    s.sim = sim;
+    s.elem = ex + h->g.nx * (ey + h->g.ny * ez);
+    s.vm.assign(vanderm, vanderm + h->NP);
+    const int nc = kind == SESNT_SOURCE_MT ? 6 : 3, off = kind == SESNT_SOURCE_MT ? 0 : 6;
+    for (int c = 0; c < 9; ++c) s.present[c] = false;
+    for (int c = 0; c < nc; ++c) {
+        std::vector<float> d(nt);
+        bool nonzero = false;
+        for (int t = 0; t < nt; ++t) {
+            d[t] = stf[t] * comp[c];  // channel data in REAL32, src/config/source.f90:307-312
+            nonzero = nonzero || d[t] != 0.0f;
+        }
+        // moment-tensor channels that are zero throughout are dropped
+        // (src/config/source.f90:318-321); force channels are all kept.
+        if (kind == SESNT_SOURCE_MT && !nonzero) continue;
+        s.present[off + c] = true;
+        s.data[off + c] = std::move(d);
+    }
+    h->sources.push_back(std::move(s));
+    h->src_dirty = true;
+    return SESNT_OK;
+}
+
+int sesnt_add_receiver(sesnt_t *h, int ex, int ey, int ez, const float *vanderm, unsigned channel_mask) {
+    if (!h) return SESNT_EINVAL;
+    if (!vanderm) return h->fail(SESNT_EINVAL, "vanderm is required");
+    if (ex < 0 || ex >= h->g.nx || ey < 0 || ey >= h->g.ny || ez < 0 || ez >= h->g.nz)
+        return h->fail(SESNT_ERANGE, "element (%d,%d,%d) outside the grid", ex, ey, ez);
+    h->rec_elem.push_back(ex + h->g.nx * (ey + h->g.ny * ez));
+    h->rec_vm.insert(h->rec_vm.end(), vanderm, vanderm + h->NP);
+    h->rec_mask.push_back(channel_mask & 7u);
+    h->rec_dirty = true;
+    return (int)h->rec_elem.size() - 1;
+}
+
+int sesnt_step(sesnt_t *h, int it) {
+    if (!h) return SESNT_EINVAL;
+    const bool g = h->use_graph;
+    h->use_graph = false;
+    int rc = run_any(h, it, 1);
+    h->use_graph = g;
+    return rc;
+}
+
+int sesnt_run(sesnt_t *h, int it0, int nsteps) {
+    if (!h) return SESNT_EINVAL;
+    return run_any(h, it0, nsteps);
+}
+
+int sesnt_run_timed(sesnt_t *h, int it0, int nsteps, float *ms) {
+    if (!h || !ms) return SESNT_EINVAL;
+    // prepare (uploads, graph) outside the timed region
+    int rc = h->dbl ? prepare_run<double>(h) : prepare_run<float>(h);
+    if (rc) return rc;
+    if (h->use_graph && nsteps >= kGraphSteps && !h->graph) {
+        rc = h->dbl ? build_graph<double>(h) : build_graph<float>(h);
+        if (rc) return rc;
+    }
+    cudaEventRecord(h->ev0, h->stream);
+    rc = run_any(h, it0, nsteps);
+    cudaEventRecord(h->ev1, h->stream);
+    cudaError_t e = cudaEventSynchronize(h->ev1);
+    if (rc) return rc;
+    if (e != cudaSuccess) return h->cuda_fail(e, "timed run");
+    cudaEventElapsedTime(ms, h->ev0, h->ev1);
+    return SESNT_OK;
+}
+
+int sesnt_run_profiled(sesnt_t *h, int it0, int nsteps, float ms[4]) {
+    if (!h || !ms) return SESNT_EINVAL;
+    for (int q = 0; q < 4; ++q) ms[q] = 0.0f;
+    if (it0 < 1 || it0 + nsteps - 1 > h->g.nt)
+        return h->fail(SESNT_ERANGE, "steps %d..%d outside 1..nt=%d", it0, it0 + nsteps - 1, h->g.nt);
+    int rc = h->dbl ? prepare_run<double>(h) : prepare_run<float>(h);
+    if (rc) return rc;
+    cudaEvent_t ev[5];
+    for (auto &e : ev) cudaEventCreate(&e);
+    k_set_it<<<1, 1, 0, h->stream>>>(h->d_it, it0);
+    cudaError_t err = cudaSuccess;
+    for (int n = 0; n < nsteps && !rc; ++n) {
+        auto launch = [&](auto tag) -> int {
+            using T = decltype(tag);
+            const LpdOps<T> *o = ops<T>(h);
+            StepArgs<T> a = h->args<T>();
+            a.step_off = n;
+            cudaEventRecord(ev[0], h->stream);
+            if (o->element(a, h->sls, h->aniso, h->stream)) return -1;
+            cudaEventRecord(ev[1], h->stream);
+            if (o->sources(a, h->stream)) return -1;
+            cudaEventRecord(ev[2], h->stream);
+            if (o->node(a, h->kahan, h->stream)) return -1;
+            cudaEventRecord(ev[3], h->stream);
+            if (o->receivers(a, h->stream)) return -1;
+            cudaEventRecord(ev[4], h->stream);
+            return 0;
+        };
+        if (h->dbl ? launch(double(0)) : launch(float(0))) {
+            rc = h->fail(SESNT_ECUDA, "kernel launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+            break;
+        }
+        err = cudaEventSynchronize(ev[4]);
+        if (err != cudaSuccess) break;
+        for (int q = 0; q < 4; ++q) {
+            float t = 0.0f;
+            cudaEventElapsedTime(&t, ev[q], ev[q + 1]);
+            ms[q] += t;
+        }
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    if (rc) return rc;
+    return err == cudaSuccess ? SESNT_OK : h->cuda_fail(err, "profiled run");
+}
+
+int sesnt_get_samples(sesnt_t *h, int it, float *out) {
+    if (!h || !out) return SESNT_EINVAL;
+    if (it < 1 || it > h->g.nt) return h->fail(SESNT_ERANGE, "step %d outside 1..%d", it, h->g.nt);
+    const size_t nrec = h->rec_elem.size();
+    if (nrec == 0) return SESNT_OK;
+    if (h->rec_dirty) return h->fail(SESNT_ESTATE, "receivers added after the last step");
+    const size_t E = h->esize, nt = h->g.nt;
+    std::vector<double> tmp(h->S * nrec * 3);
+    // one strided 2-D copy: rows [s][r][c] of the seismogram array, column it-1
+    cudaError_t e = cudaMemcpy2DAsync(tmp.data(), E, (const char *)h->d_seis + (size_t)(it - 1) * E, nt * E, E,
+                                      (size_t)h->S * nrec * 3, cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "reading samples");
+    for (size_t x = 0; x < tmp.size(); ++x) {
+        const size_t r = (x / 3) % nrec;
+        const bool on = (h->rec_mask[r] >> (x % 3)) & 1u;
+        float v;
+        if (E == 8) v = (float)tmp[x];
+        else std::memcpy(&v, (const char *)tmp.data() + x * 4, 4);
+        out[x] = on ? v : 0.0f;
+    }
+    return SESNT_OK;
+}
+
+int sesnt_synchronize(sesnt_t *h) {
+    if (!h) return SESNT_EINVAL;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    return e == cudaSuccess ? SESNT_OK : h->cuda_fail(e, "synchronize");
+}
+
+int sesnt_reset(sesnt_t *h) {
+    if (!h) return SESNT_EINVAL;
+    int rc = zero_state(h);
+    if (rc) return rc;
+    return sesnt_synchronize(h);
+}
+
+int sesnt_get_seismograms(sesnt_t *h, float *out) {
+    if (!h || !out) return SESNT_EINVAL;
+    return h->dbl ? get_seis_impl<double>(h, out) : get_seis_impl<float>(h, out);
+}
+
+int sesnt_get_field(sesnt_t *h, int sim, int which, void *out, int out_precision) {
+    if (!h || !out) return SESNT_EINVAL;
+    if (sim < 0 || sim >= h->S) return h->fail(SESNT_ERANGE, "simulation %d outside 0..%d", sim, h->S - 1);
+    if (out_precision != 4 && out_precision != 8) return h->fail(SESNT_EINVAL, "out_precision must be 4 or 8");
+    if (!h->model_set && which != SESNT_FIELD_TAPER)
+        return h->fail(SESNT_ESTATE, "sesnt_set_model must be called first");
+    return h->dbl ? get_field_impl<double>(h, sim, which, out, out_precision)
+                  : get_field_impl<float>(h, sim, which, out, out_precision);
+}
+
+int sesnt_v_ptp(sesnt_t *h, int sim, float out[2]) {
+    if (!h || !out) return SESNT_EINVAL;
+    if (sim < 0 || sim >= h->S) return h->fail(SESNT_ERANGE, "simulation %d outside 0..%d", sim, h->S - 1);
+    return h->dbl ? v_ptp_impl<double>(h, sim, out) : v_ptp_impl<float>(h, sim, out);
+}
+
+int sesnt_assemble_field(sesnt_t *h, float *field) {
+    if (!h || !field) return SESNT_EINVAL;
+    return h->dbl ? assemble_impl<double>(h, field) : assemble_impl<float>(h, field);
+}
+
+int sesnt_info(const sesnt_t *h, long long out[6]) {
+    if (!h || !out) return SESNT_EINVAL;
+    out[0] = h->nel;
+    out[1] = h->nloc;
+    out[2] = h->nuni;
+    out[3] = (long long)h->dev_bytes;
+    out[4] = algorithmic_bytes(h->nloc, h->nuni, h->sls ? kNsls : 0, h->aniso, h->S, h->esize);
+    out[5] = 2 + (h->nsrc_rec > 0 || !h->sources.empty() ? 1 : 0) + (h->rec_elem.empty() ? 0 : 1);
+    return SESNT_OK;
+}
+
+long long sesnt_footprint_bytes(const sesnt_grid_t *grid) {
+    std::string why;
+    if (check_grid(grid, why)) return -1;
+    return (long long)footprint(grid, false);
+}
+
+void *sesnt_stream(const sesnt_t *h) { return h ? (void *)h->stream : nullptr; }
+
+}  // extern "C"

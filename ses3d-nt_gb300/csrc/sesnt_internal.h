@@ -1,0 +1,139 @@
+// Internal declarations shared by the host set-up code, the kernels and the
+// C ABI implementation.
+//
+// Device data layout (one handle, `batch` = S simulations sharing a model):
+//   element-local arrays  x[e*NP + p]      e = ex + nx*(ey + ny*ez),
+//                                          p = i + P*(j + P*k), P = lpd+1,
+//                                          NP = P^3 (an element's points are
+//                                          contiguous, so a thread block that
+//                                          owns a few elements streams one
+//                                          contiguous range per component)
+//   per-simulation blocks sigma[s][6][N_loc], memory[s][6*n_sls][N_loc]
+//   unique-point arrays   v[s][3][N_uni], force[s][3][N_uni], inv_mass[N_uni]
+//                         u = gx + NXU*(gy + NYU*gz), gx = ex*lpd + i, ...
+// The unique numbering is arithmetic (structured grid), so assembly needs no
+// connectivity array: every element computes the unique index of its points.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace sesnt {
+
+constexpr int kMaxLpd = 7;
+constexpr int kMinLpd = 2;
+constexpr int kNsls = 3;  // relaxation mechanisms, src/geometric_paras.f90:41
+
+// Relaxation times tau_p [s], src/geometric_paras.f90:42.
+constexpr double kTauP[kNsls] = {1000.00, 70.00, 5.25};
+
+// One source channel set resolved for one (simulation, element): for each of
+// the 9 components (mxx mxy mxz myy myz mzz fx fy fz) the index of the
+// Vandermonde row and of the data row to use, or -1.
+struct SrcRec {
+    int sim;
+    int elem;
+    int vm[9];
+    int data[9];
+};
+
+template <typename T>
+struct StepArgs {
+    // grid
+    int nx, ny, nz, nel, S;
+    int NXU, NYU, NZU;
+    long long nuni, nloc;
+    T dt, c1, c2, c3, jac, alpha;
+    T tau_p[kNsls];
+    // small tables (device): tabD = [Dx | Dy | Dz | Dt], each P*P
+    const T *tabD, *w, *sin_t, *cot_t, *r, *px, *py, *pz;
+    // model (element-local)
+    const T *lam, *mu, *A, *B, *C, *tau;
+    // state
+    T *sig, *mem, *v, *vc, *F;
+    const T *invM;
+    // sources
+    int nsrc, nt;
+    const SrcRec *src;
+    const T *src_vm;    // [n_vm][NP]
+    const T *src_data;  // [n_data][nt]
+    // receivers
+    int nrec;
+    const int *rec_elem;
+    const T *rec_vm;    // [nrec][NP]
+    T *seis;            // [S][nrec][3][nt]
+    // step counter: it = *d_it + step_off
+    const int *d_it;
+    int step_off;
+};
+
+// Kernel launchers for one polynomial degree and one precision, filled in by
+// the per-degree translation units.
+template <typename T>
+struct LpdOps {
+    int (*element)(const StepArgs<T> &, bool sls, bool aniso, void *stream);
+    int (*node)(const StepArgs<T> &, bool kahan, void *stream);
+    int (*sources)(const StepArgs<T> &, void *stream);
+    int (*receivers)(const StepArgs<T> &, void *stream);
+    // FP64 inverse mass per unique point from element-local rhoinv and the
+    // FP64 metric tables sin(theta)[nx*P], r[nz*P], GLL weights[P].
+    int (*inv_mass)(const StepArgs<T> &, const T *rhoinv_loc, const double *dsin, const double *dr,
+                    const double *dw, double jac, void *stream);
+    // element-local copy of a unique-point field (for get_field), T -> T.
+    int (*gather_local)(const StepArgs<T> &, const T *uni, T *loc, void *stream);
+    // sum element-local copies into unique points, T (for assemble_field).
+    int (*scatter_unique)(const StepArgs<T> &, const T *loc, T *uni, void *stream);
+    // element-local taper (for get_field).
+    int (*taper_local)(const StepArgs<T> &, T *loc, void *stream);
+    int threads_element;
+    size_t smem_element;
+};
+
+template <int N, typename T>
+const LpdOps<T> *lpd_ops_n();  // defined in kern_lpd<N>.cu
+
+template <typename T>
+const LpdOps<T> *lpd_ops(int lpd);
+
+// ---------------------------------------------------------------------------
+// Host set-up (setup.cpp). Float32 routines reproduce the reference's FP32
+// formula order; the templated ones are evaluated in the requested precision.
+// ---------------------------------------------------------------------------
+template <typename T>
+std::vector<T> gll_points(int lpd);
+template <typename T>
+std::vector<T> gll_quadrature_weights(int lpd);
+template <typename T>
+std::vector<T> lagrange_derivative_matrix(int lpd);  // d[i*P+j] = l_i'(xi_j)
+
+template <typename T>
+struct Domain {
+    T x_glb_min, x_glb_max, y_glb_min, y_glb_max, z_glb_min, z_glb_max;
+    T dx_elm, dy_elm, dz_elm;
+    T x_loc_min, x_loc_max, y_loc_min, y_loc_max, z_loc_min, z_loc_max;
+};
+template <typename T>
+Domain<T> make_domain(int nx, int ny, int nz, float lat_min, float lat_max, float lon_min, float lon_max,
+                      float rad_min, float rad_max);
+
+template <typename T>
+std::vector<T> element_coordinates(int elms, int lpd, T lo, T hi);  // [e*P+n]
+
+// Damping profiles of the absorbing taper (before corner normalisation),
+// one 1-D table per direction indexed [e*P+n].
+template <typename T>
+void taper_profiles(int nx, int ny, int nz, int lpd, int width, T alpha, const Domain<T> &d, std::vector<T> &px,
+                    std::vector<T> &py, std::vector<T> &pz);
+
+int locate_point(int nx, int ny, int nz, int lpd, float lat_min, float lat_max, float lon_min, float lon_max,
+                 float rad_min, float rad_max, float lat, float lon, float depth, int elem[3], float *vanderm,
+                 std::string &why);
+
+int source_signature(int wavelet, float onset, float width, float dt, int nt, float *out);
+
+// Algorithmic HBM bytes of one time step (the fixed formula of the roofline).
+long long algorithmic_bytes(long long nloc, long long nuni, int n_sls, bool aniso, int S, int elem_bytes);
+
+}  // namespace sesnt

@@ -1,0 +1,302 @@
+"""Python binding of libsesnt (include/sesnt.h) through ctypes.
+
+This is the host-side mirror of the reference driver's interface for the time
+step: a `Simulation` owns one library handle (one Earth model, `batch`
+simulations) and exposes the calls the Fortran driver makes around
+`ses3d_evolution` (src/ses3d-nt.F90:84-275): model set-up, point location,
+sources, receivers, stepping and readback. Arrays use the reference raw
+layout: numpy arrays of shape (nx, ny, nz, lpd+1, lpd+1, lpd+1) in Fortran
+order (element x index fastest).
+
+There is no CPU path: if libsesnt.so is missing or was built without a GPU
+visible, every call fails with a clear error.
+"""
+import ctypes as C
+import os
+import re
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsesnt.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "sesnt.h")
+
+OK = 0
+EINVAL, ECUDA, ENOMEM, ESTATE, ERANGE, ETIMEOUT, ENOTFOUND, EUNSUPPORTED, ENONFINITE = range(-1, -10, -1)
+FLAG_KAHAN = 1
+FLAG_NO_GRAPH = 2
+SOURCE_MT, SOURCE_SF = 0, 1
+WAVELETS = {"DELTA": 0, "RICKER": 1, "GAUSS": 2, "SIN**3": 3, "BRUNE": 4}
+CH_VX, CH_VY, CH_VZ = 1, 2, 4
+FIELDS = {"vx": 0, "vy": 1, "vz": 2, "sxx": 3, "sxy": 4, "sxz": 5, "syy": 6, "syz": 7, "szz": 8,
+          "taper": 9, "mass": 10}
+MEMORY_FIELD0 = 13
+
+
+class SesntError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("sesnt error %d: %s" % (code, msg))
+        self.code = code
+
+
+class _Grid(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("lpd", C.c_int),
+                ("taper_width", C.c_int), ("taper_slope", C.c_float),
+                ("lat_min", C.c_float), ("lat_max", C.c_float), ("lon_min", C.c_float),
+                ("lon_max", C.c_float), ("rad_min", C.c_float), ("rad_max", C.c_float),
+                ("dt", C.c_float), ("nt", C.c_int), ("n_sls", C.c_int), ("precision", C.c_int),
+                ("batch", C.c_int), ("flags", C.c_uint)]
+
+
+@dataclass
+class Grid:
+    """Values of the reference NAMELIST groups &grid, &model, &time plus the
+    GPU build choices (n_sls, precision, batch, flags)."""
+    nx: int
+    ny: int
+    nz: int
+    lpd: int
+    lat_min: float
+    lat_max: float
+    lon_min: float
+    lon_max: float
+    rad_min: float
+    rad_max: float
+    dt: float
+    nt: int
+    taper_width: int = 3
+    taper_slope: float = 1.2
+    n_sls: int = 0
+    precision: int = 4
+    batch: int = 1
+    flags: int = 0
+
+    def c(self):
+        return _Grid(self.nx, self.ny, self.nz, self.lpd, self.taper_width, self.taper_slope,
+                     self.lat_min, self.lat_max, self.lon_min, self.lon_max, self.rad_min,
+                     self.rad_max, self.dt, self.nt, self.n_sls, self.precision, self.batch,
+                     self.flags)
+
+    @property
+    def shape(self):
+        p = self.lpd + 1
+        return (self.nx, self.ny, self.nz, p, p, p)
+
+    @property
+    def n_loc(self):
+        return self.nx * self.ny * self.nz * (self.lpd + 1) ** 3
+
+    @property
+    def n_uni(self):
+        n = self.lpd
+        return (self.nx * n + 1) * (self.ny * n + 1) * (self.nz * n + 1)
+
+
+_lib = None
+
+
+def header_functions():
+    """Names of every function declared in include/sesnt.h."""
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(sesnt_[a-z_0-9]+)\s*\(", txt)))
+
+
+def lib():
+    """Load libsesnt.so (built in place by build.py)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise SesntError(EUNSUPPORTED, "libsesnt.so not found at %s; run __graft_entry__.build()" % LIB_PATH)
+    L = C.CDLL(LIB_PATH)
+    P, I, F, U = C.c_void_p, C.c_int, C.c_float, C.c_uint
+    fp = C.POINTER(C.c_float)
+    ip = C.POINTER(C.c_int)
+    G = C.POINTER(_Grid)
+    sig = {
+        "sesnt_create": (I, [G, C.POINTER(C.c_void_p)]),
+        "sesnt_destroy": (I, [P]),
+        "sesnt_last_error": (C.c_char_p, [P]),
+        "sesnt_set_model": (I, [P, fp, fp, fp, fp, fp, fp, fp]),
+        "sesnt_locate_point": (I, [G, F, F, F, ip, fp]),
+        "sesnt_source_signature": (I, [I, F, F, F, I, fp]),
+        "sesnt_add_source": (I, [P, I, I, I, I, fp, I, fp, fp, I]),
+        "sesnt_add_receiver": (I, [P, I, I, I, fp, U]),
+        "sesnt_step": (I, [P, I]),
+        "sesnt_run": (I, [P, I, I]),
+        "sesnt_run_timed": (I, [P, I, I, fp]),
+        "sesnt_synchronize": (I, [P]),
+        "sesnt_run_profiled": (I, [P, I, I, fp]),
+        "sesnt_get_samples": (I, [P, I, fp]),
+        "sesnt_reset": (I, [P]),
+        "sesnt_get_seismograms": (I, [P, fp]),
+        "sesnt_get_field": (I, [P, I, I, P, I]),
+        "sesnt_v_ptp": (I, [P, I, fp]),
+        "sesnt_assemble_field": (I, [P, fp]),
+        "sesnt_info": (I, [P, C.POINTER(C.c_longlong)]),
+        "sesnt_footprint_bytes": (C.c_longlong, [G]),
+        "sesnt_stream": (P, [P]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _fptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _f32(a, n=None):
+    a = np.ascontiguousarray(np.asarray(a, dtype=np.float32).ravel(order="F") if np.ndim(a) > 1
+                             else np.asarray(a, dtype=np.float32))
+    if n is not None and a.size != n:
+        raise ValueError("expected %d values, got %d" % (n, a.size))
+    return a
+
+
+def _check(rc, h=None):
+    if rc < 0:
+        msg = lib().sesnt_last_error(h)
+        raise SesntError(rc, msg.decode() if msg else "")
+    return rc
+
+
+def locate_point(grid, lat, lon, depth):
+    """(ex, ey, ez), vanderm[(lpd+1)^3] for a point (construct_point_cls)."""
+    p = grid.lpd + 1
+    elem = (C.c_int * 3)()
+    vm = np.zeros(p ** 3, np.float32)
+    g = grid.c()
+    _check(lib().sesnt_locate_point(C.byref(g), lat, lon, depth, elem, _fptr(vm)))
+    return (elem[0], elem[1], elem[2]), vm
+
+
+def source_signature(wavelet, onset, width, dt, nt):
+    code = WAVELETS[wavelet] if isinstance(wavelet, str) else int(wavelet)
+    out = np.zeros(nt, np.float32)
+    _check(lib().sesnt_source_signature(code, onset, width, dt, nt, _fptr(out)))
+    return out
+
+
+def footprint_bytes(grid):
+    g = grid.c()
+    return lib().sesnt_footprint_bytes(C.byref(g))
+
+
+class Simulation:
+    """One handle: an Earth model on the GPU and `grid.batch` wavefields."""
+
+    def __init__(self, grid):
+        self.grid = grid
+        self._h = C.c_void_p()
+        g = grid.c()
+        _check(lib().sesnt_create(C.byref(g), C.byref(self._h)))
+        self.receivers = 0
+
+    def close(self):
+        if self._h:
+            lib().sesnt_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def _c(self, rc):
+        return _check(rc, self._h)
+
+    def set_model(self, rhoinv, lam, mu, a=None, b=None, c=None, q=None):
+        n = self.grid.n_loc
+        arrs = [None if x is None else _f32(x, n) for x in (rhoinv, lam, mu, a, b, c, q)]
+        ptrs = [None if x is None else _fptr(x) for x in arrs]
+        self._c(lib().sesnt_set_model(self._h, *ptrs))
+
+    def add_source(self, sim, elem, vanderm, kind, comp, stf):
+        vm = _f32(vanderm, (self.grid.lpd + 1) ** 3)
+        cp = _f32(comp)
+        st = _f32(stf, self.grid.nt)
+        self._c(lib().sesnt_add_source(self._h, sim, elem[0], elem[1], elem[2], _fptr(vm), kind, _fptr(cp),
+                                       _fptr(st), st.size))
+
+    def add_receiver(self, elem, vanderm, channels=CH_VX | CH_VY | CH_VZ):
+        vm = _f32(vanderm, (self.grid.lpd + 1) ** 3)
+        r = self._c(lib().sesnt_add_receiver(self._h, elem[0], elem[1], elem[2], _fptr(vm), channels))
+        self.receivers += 1
+        return r
+
+    def step(self, it):
+        self._c(lib().sesnt_step(self._h, it))
+
+    def run(self, it0, nsteps):
+        self._c(lib().sesnt_run(self._h, it0, nsteps))
+
+    def run_timed(self, it0, nsteps):
+        ms = C.c_float()
+        self._c(lib().sesnt_run_timed(self._h, it0, nsteps, C.byref(ms)))
+        return ms.value
+
+    def run_profiled(self, it0, nsteps):
+        """Device milliseconds summed per kernel: element, sources, node, receivers."""
+        ms = np.zeros(4, np.float32)
+        self._c(lib().sesnt_run_profiled(self._h, it0, nsteps, _fptr(ms)))
+        return ms
+
+    def samples(self, it, out=None):
+        """Receiver samples of step it, [batch][nrec][3]."""
+        if out is None:
+            out = np.zeros((self.grid.batch, self.receivers, 3), np.float32)
+        if self.receivers:
+            self._c(lib().sesnt_get_samples(self._h, it, _fptr(out)))
+        return out
+
+    def synchronize(self):
+        self._c(lib().sesnt_synchronize(self._h))
+
+    def reset(self):
+        self._c(lib().sesnt_reset(self._h))
+
+    def seismograms(self):
+        out = np.zeros((self.grid.batch, self.receivers, 3, self.grid.nt), np.float32)
+        if self.receivers:
+            self._c(lib().sesnt_get_seismograms(self._h, _fptr(out)))
+        return out
+
+    def field(self, which, sim=0, precision=4):
+        code = FIELDS[which] if isinstance(which, str) else int(which)
+        dt = np.float64 if precision == 8 else np.float32
+        out = np.zeros(self.grid.n_loc, dt)
+        self._c(lib().sesnt_get_field(self._h, sim, code, out.ctypes.data_as(C.c_void_p), precision))
+        return out.reshape(self.grid.shape, order="F")
+
+    def v_ptp(self, sim=0):
+        out = np.zeros(2, np.float32)
+        self._c(lib().sesnt_v_ptp(self._h, sim, _fptr(out)))
+        return float(out[0]), float(out[1])
+
+    def assemble(self, field):
+        f = _f32(field, self.grid.n_loc).copy()
+        self._c(lib().sesnt_assemble_field(self._h, _fptr(f)))
+        return f.reshape(self.grid.shape, order="F")
+
+    def info(self):
+        out = (C.c_longlong * 6)()
+        self._c(lib().sesnt_info(self._h, out))
+        keys = ("elements", "n_loc", "n_uni", "device_bytes", "algorithmic_bytes_per_step", "launches_per_step")
+        return dict(zip(keys, list(out)))

@@ -1,0 +1,286 @@
+"""Parity of the sm_103a time step with the oracle, called through the C ABI.
+
+Tolerances (FP32 wavefields): seismograms and final wavefields within 1e-4
+relative L2 of the oracle; the assembly of shared points bit-exact on
+integer data; derived set-up fields (taper, mass matrix) within a few float32
+ulps. Each test also states the FP32 error against the FP64 build of the same
+GPU code where that is meaningful.
+"""
+import copy
+
+import numpy as np
+import pytest
+
+import sesnt
+import workloads
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    nb = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / nb) if nb > 0 else float(np.linalg.norm(a))
+
+
+def with_grid(wl, **kw):
+    w = copy.copy(wl)
+    w.grid = copy.copy(wl.grid)
+    for k, v in kw.items():
+        setattr(w.grid, k, v)
+    return w
+
+
+def run_gpu(wl, nsteps, fields=("vx", "vy", "vz", "sxx", "syz"), chunked=False):
+    with sesnt.Simulation(wl.grid) as sim:
+        workloads.setup(sim, wl)
+        if chunked:
+            it = 1
+            while it <= nsteps:
+                n = min(37, nsteps - it + 1)
+                sim.run(it, n)
+                it += n
+        else:
+            sim.run(1, nsteps)
+        seis = sim.seismograms()
+        f = {k: sim.field(k, sim=0) for k in fields}
+        ptp = sim.v_ptp(0)
+    return seis, f, ptp
+
+
+def run_oracle(oracle_mod, wl, nsteps, sim=0, precision=4):
+    o = oracle_mod.Oracle(wl.grid, precision)
+    oracle_mod.load_workload(o, wl, sim=sim)
+    o.run(nsteps)
+    names = {"vx": 0, "vy": 1, "vz": 2, "sxx": 3, "sxy": 4, "sxz": 5, "syy": 6, "syz": 7, "szz": 8}
+    return o.seismograms(), {k: o.field(v) for k, v in names.items()}, o
+
+
+def small_workload(lpd, n_sls=0, aniso=False, seed=1, kind=sesnt.SOURCE_MT, nt=300, nx=6, ny=6, nz=5):
+    g = sesnt.Grid(nx=nx, ny=ny, nz=nz, lpd=lpd, lat_min=30.0, lat_max=40.0, lon_min=0.0, lon_max=10.0,
+                   rad_min=5971000.0, rad_max=6371000.0, dt=0.1, nt=nt, taper_width=1, taper_slope=1.2,
+                   n_sls=n_sls)
+    model = workloads.gradient_model(g, seed, q=n_sls > 0)
+    if aniso:
+        rng = np.random.default_rng(seed + 100)
+        mu = model["mu"]
+        for key in ("a", "b", "c"):
+            model[key] = np.asfortranarray((0.02 * mu * rng.uniform(-1, 1, size=mu.shape)).astype(np.float32))
+    comp = (1e18, 0.3e18, -0.2e18, 0.8e18, 0.1e18, 1.2e18) if kind == sesnt.SOURCE_MT else (1e15, -2e15, 3e15)
+    src = [workloads.Source(lat=35.3, lon=4.6, depth=90000.0, kind=kind, comp=comp, width=8.0, onset=12.0)]
+    rec = [workloads.Receiver(lat=32.5 + 1.2 * q, lon=2.5 + 1.0 * q, depth=0.0) for q in range(5)]
+    rec += [workloads.Receiver(lat=35.0, lon=5.0, depth=150000.0)]
+    return workloads.Workload("small_lpd%d" % lpd, g, model, src, rec)
+
+
+@pytest.fixture(scope="module")
+def config1_runs(gpu, sesnt_lib, oracle_mod):
+    wl = workloads.config1(nt=2000)
+    gs, gf, ptp = run_gpu(wl, 2000)
+    os_, of, _ = run_oracle(oracle_mod, wl, 2000)
+    g64, f64, _ = run_gpu(with_grid(wl, precision=8), 2000)
+    return wl, (gs, gf, ptp), (os_, of), (g64, f64)
+
+
+def test_config1_seismograms(config1_runs):
+    wl, (gs, gf, ptp), (os_, of), (g64, f64) = config1_runs
+    e = rel_l2(gs[0], os_)
+    e64 = rel_l2(gs[0], g64[0])
+    eo64 = rel_l2(os_, g64[0])
+    print("config1 2000 steps: seismograms GPU-FP32 vs oracle %.2e, vs GPU-FP64 %.2e; oracle vs GPU-FP64 %.2e"
+          % (e, e64, eo64))
+    assert np.abs(os_).max() > 0
+    assert e < TOL
+    for c in range(3):
+        assert rel_l2(gs[0][:, c], os_[:, c]) < TOL
+    assert e64 < TOL
+
+
+def test_config1_final_wavefield(config1_runs):
+    wl, (gs, gf, ptp), (os_, of), (g64, f64) = config1_runs
+    for k in gf:
+        e = rel_l2(gf[k], of[k])
+        print("config1 final %s: vs oracle %.2e, vs FP64 %.2e" % (k, e, rel_l2(gf[k], f64[k])))
+        assert e < TOL, k
+    # v_ptp (src/elastic_vars.F90:179-213) equals min/max of the velocity field
+    vmin = min(of["vx"].min(), of["vy"].min(), of["vz"].min())
+    vmax = max(of["vx"].max(), of["vy"].max(), of["vz"].max())
+    scale = max(abs(vmin), abs(vmax))
+    assert abs(ptp[0] - vmin) < 1e-3 * scale and abs(ptp[1] - vmax) < 1e-3 * scale
+
+
+@pytest.mark.parametrize("lpd", [2, 3, 4, 5, 6, 7])
+def test_degrees_heterogeneous_elastic(gpu, sesnt_lib, oracle_mod, lpd):
+    wl = small_workload(lpd, nt=300)
+    gs, gf, _ = run_gpu(wl, 300)
+    os_, of, _ = run_oracle(oracle_mod, wl, 300)
+    e = rel_l2(gs[0], os_)
+    print("lpd %d seismograms vs oracle %.2e" % (lpd, e))
+    assert np.abs(os_).max() > 0
+    assert e < TOL
+    for k in ("vx", "vz", "sxx"):
+        assert rel_l2(gf[k], of[k]) < TOL, k
+
+
+@pytest.mark.parametrize("lpd", [4, 6])
+def test_visco_elastic_sls(gpu, sesnt_lib, oracle_mod, lpd):
+    wl = small_workload(lpd, n_sls=3, nt=400)
+    with sesnt.Simulation(wl.grid) as sim:
+        workloads.setup(sim, wl)
+        sim.run(1, 400)
+        gs = sim.seismograms()
+        mem = [sim.field(sesnt.MEMORY_FIELD0 + c * 3 + q) for c in (0, 3) for q in range(3)]
+        vz = sim.field("vz")
+    os_, of, o = run_oracle(oracle_mod, wl, 400)
+    assert o.visco()
+    e = rel_l2(gs[0], os_)
+    print("SLS lpd %d seismograms vs oracle %.2e" % (lpd, e))
+    assert e < TOL
+    assert rel_l2(vz, of["vz"]) < TOL
+    omem = [o.field(13 + c * 3 + q) for c in (0, 3) for q in range(3)]
+    for a, b in zip(mem, omem):
+        assert np.abs(b).max() > 0
+        assert rel_l2(a, b) < 10 * TOL
+    # attenuation changes the seismograms
+    el = small_workload(lpd, n_sls=0, nt=400)
+    ge, _, _ = run_gpu(el, 400)
+    assert rel_l2(ge[0], gs[0]) > 1e-3
+
+
+def test_anisotropy_and_single_force(gpu, sesnt_lib, oracle_mod):
+    for kind in (sesnt.SOURCE_MT, sesnt.SOURCE_SF):
+        wl = small_workload(4, aniso=True, kind=kind, nt=300)
+        gs, gf, _ = run_gpu(wl, 300)
+        os_, of, _ = run_oracle(oracle_mod, wl, 300)
+        e = rel_l2(gs[0], os_)
+        print("aniso kind %d seismograms vs oracle %.2e" % (kind, e))
+        assert np.abs(os_).max() > 0
+        assert e < TOL
+
+
+def test_batch_matches_independent_runs(gpu, sesnt_lib, oracle_mod):
+    wl = small_workload(4, nt=300)
+    g = copy.copy(wl.grid)
+    g.batch = 3
+    srcs = []
+    for s in range(3):
+        src = copy.copy(wl.sources[0])
+        src.sim = s
+        src.lat = 34.0 + s
+        src.lon = 3.5 + 1.5 * s
+        src.comp = tuple((1.0 + 0.5 * s) * c for c in src.comp)
+        srcs.append(src)
+    bw = workloads.Workload("batch3", g, wl.model, srcs, wl.receivers)
+    gs, _, _ = run_gpu(bw, 300, fields=())
+    for s in range(3):
+        one = workloads.Workload("one", wl.grid, wl.model, [copy.copy(srcs[s])], wl.receivers)
+        one.sources[0].sim = 0
+        os_, _, _ = run_oracle(oracle_mod, one, 300)
+        e = rel_l2(gs[s], os_)
+        print("batch member %d vs oracle %.2e" % (s, e))
+        assert e < TOL
+
+
+def test_two_sources_in_one_element_overwrite(gpu, sesnt_lib, oracle_mod):
+    """Sources assign element slabs, so a later source in the same element
+    replaces the earlier one channel by channel (channel_mod.f90:866-867)."""
+    wl = small_workload(4, nt=250)
+    s2 = copy.copy(wl.sources[0])
+    s2.lat += 0.05
+    s2.comp = (0.0, 2e18, 0.0, 0.0, 0.0, -1e18)  # overrides mxy and mzz only
+    s3 = copy.copy(wl.sources[0])
+    s3.kind = sesnt.SOURCE_SF
+    s3.comp = (1e15, 0.0, 0.0)
+    wl.sources = [wl.sources[0], s2, s3]
+    gs, _, _ = run_gpu(wl, 250, fields=())
+    os_, _, _ = run_oracle(oracle_mod, wl, 250)
+    assert rel_l2(gs[0], os_) < TOL
+
+
+def test_graph_and_chunked_runs_agree(gpu, sesnt_lib):
+    wl = small_workload(4, nt=200)
+    a, _, _ = run_gpu(wl, 200)
+    b, _, _ = run_gpu(wl, 200, chunked=True)
+    wl2 = with_grid(wl, flags=sesnt.FLAG_NO_GRAPH)
+    c, _, _ = run_gpu(wl2, 200)
+    assert rel_l2(b, a) < 1e-5 and rel_l2(c, a) < 1e-5
+
+
+def test_kahan_update(gpu, sesnt_lib, oracle_mod):
+    wl = small_workload(4, nt=300)
+    k, _, _ = run_gpu(with_grid(wl, flags=sesnt.FLAG_KAHAN), 300)
+    d, _, _ = run_gpu(with_grid(wl, precision=8), 300)
+    p, _, _ = run_gpu(wl, 300)
+    ek, ep = rel_l2(k, d), rel_l2(p, d)
+    print("vs FP64: plain FP32 %.2e, Kahan FP32 %.2e" % (ep, ek))
+    assert ek < TOL and ep < TOL
+
+
+def test_assembly_bit_exact(gpu, sesnt_lib, oracle_mod):
+    for lpd in (2, 4, 7):
+        wl = small_workload(lpd, nt=4, nx=5, ny=4, nz=6)
+        rng = np.random.default_rng(lpd)
+        f = np.asfortranarray(rng.integers(-1 << 12, 1 << 12, size=wl.grid.shape).astype(np.float32))
+        with sesnt.Simulation(wl.grid) as sim:
+            got = sim.assemble(f)
+        assert np.array_equal(got, oracle_mod.assemble(f, wl.grid))
+
+
+def test_setup_fields(gpu, sesnt_lib, oracle_mod):
+    wl = workloads.config1(nt=4)
+    with sesnt.Simulation(wl.grid) as sim:
+        workloads.setup(sim, wl)
+        taper = sim.field("taper")
+        mass = sim.field("mass")
+    o = oracle_mod.Oracle(wl.grid)
+    oracle_mod.load_workload(o, wl)
+    t_ref, m_ref = o.field(9), o.field(10)
+    assert np.max(np.abs(taper - t_ref)) < 4e-7
+    assert np.max(np.abs(mass / m_ref - 1.0)) < 2e-6
+
+
+def test_state_errors(gpu, sesnt_lib):
+    wl = small_workload(4, nt=50)
+    with sesnt.Simulation(wl.grid) as sim:
+        with pytest.raises(sesnt.SesntError) as e:
+            sim.step(1)
+        assert e.value.code == sesnt.ESTATE
+        workloads.setup(sim, wl)
+        with pytest.raises(sesnt.SesntError) as e:
+            sim.run(40, 20)
+        assert e.value.code == sesnt.ERANGE
+        with pytest.raises(sesnt.SesntError) as e:
+            sim.field("vx", sim=1)
+        assert e.value.code == sesnt.ERANGE
+        sim.run(1, 50)
+        assert np.isfinite(sim.seismograms()).all()
+
+
+def test_blow_up_is_reported_not_faulted(gpu, sesnt_lib):
+    """An unstable time step (Courant number far above 1) drives the field to
+    Inf/NaN; the watchdog reports it as an error status."""
+    wl = small_workload(4, nt=400)
+    wl = with_grid(wl, dt=5.0)
+    with sesnt.Simulation(wl.grid) as sim:
+        workloads.setup(sim, wl)
+        sim.run(1, 400)
+        with pytest.raises(sesnt.SesntError) as e:
+            sim.v_ptp(0)
+        assert e.value.code == sesnt.ENONFINITE
+
+
+def test_model_validation(gpu, sesnt_lib):
+    wl = small_workload(4, nt=10)
+    m = wl.model
+    with sesnt.Simulation(wl.grid) as sim:
+        bad = m["rhoinv"].copy()
+        bad[0, 0, 0, 0, 0, 0] = 0.0
+        with pytest.raises(sesnt.SesntError) as e:
+            sim.set_model(bad, m["lambda"], m["mu"])
+        assert e.value.code == sesnt.EINVAL
+        q = np.full(wl.grid.shape, 100.0, np.float32)
+        with pytest.raises(sesnt.SesntError):
+            sim.set_model(m["rhoinv"], m["lambda"], m["mu"], q=q)  # elastic handle, q given

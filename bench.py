@@ -258,8 +258,9 @@ def run_ours(args):
     }
     if prof is not None:
         eb = element_kernel_bytes(g, aniso)
-        t_el = prof[0] / KP / 1e3
+        t_el = float(prof[0]) / KP / 1e3
         ach = eb / t_el / 1e9
+        prof = [float(x) for x in prof]
         line["kernels_ms_per_step"] = {"element": prof[0] / KP, "sources": prof[1] / KP, "node": prof[2] / KP,
                                        "receivers": prof[3] / KP}
         traffic = None

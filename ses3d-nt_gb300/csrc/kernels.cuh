@@ -37,6 +37,8 @@ struct ElemCfg {
     // elements per block: enough points to fill whole warps with little waste
     static constexpr int EPB = NP <= 32 ? 8 : (NP <= 64 ? 2 : (NP <= 128 ? 2 : 1));
     static constexpr int NT = ((EPB * NP + 31) / 32) * 32;
+    // resident blocks per SM the register allocation is sized for
+    static constexpr int MINB = NT <= 256 ? 4 : (NT <= 384 ? 2 : 1);
 };
 
 template <typename T>
@@ -51,17 +53,16 @@ __device__ __forceinline__ void st_stream(T *p, T v) {
 // Taper from the three damping profiles (src/geometric_paras.f90:308-316):
 // corner normalisation, then exp(-0.1*prof^2).
 template <typename T>
-__device__ __forceinline__ T taper_value(T px, T py, T pz, T alpha) {
-    T prof = px + py + pz;
-    T den = T(1) + prof / alpha;
-    T qx = T(2) * px / den, qy = T(2) * py / den, qz = T(2) * pz / den;
-    T p2 = qx + qy + qz;
-    if (p2 == T(0)) return T(1);
+__device__ __forceinline__ T taper_value(T px, T py, T pz, T inv_alpha) {
+    const T prof = px + py + pz;
+    if (prof == T(0)) return T(1);
+    const T s = T(2) / (T(1) + prof * inv_alpha);
+    const T p2 = (px + py + pz) * s;
     return exp(-(T(0.1) * (p2 * p2)));
 }
 
 template <int N, typename T, int NSLS, bool ANISO>
-__global__ void __launch_bounds__(ElemCfg<N>::NT) k_element(const StepArgs<T> a) {
+__global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::MINB : 1) k_element(const StepArgs<T> a) {
     constexpr int P = ElemCfg<N>::P, NP = ElemCfg<N>::NP, EPB = ElemCfg<N>::EPB, NT = ElemCfg<N>::NT;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *sD = reinterpret_cast<T *>(smem_raw);  // [4][P*P]
@@ -82,7 +83,14 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT) k_element(const StepArgs<T> a)
     int ex = 0, ey = 0, ez = 0;
     size_t u = 0;
     const size_t nuni = (size_t)a.nuni, nloc = (size_t)a.nloc;
-    T vx = 0, vy = 0, vz = 0;
+    const size_t li = (size_t)e * NP + p;
+    // Every global load of the step is issued here, before any store, so the
+    // loads overlap each other and the line contractions below.
+    T vx = 0, vy = 0, vz = 0, lam = 0, mu = 0, tau = 0, cA = 0, cB = 0, cC = 0;
+    T sg[6] = {0, 0, 0, 0, 0, 0};
+    T m[NSLS > 0 ? 6 : 1][NSLS > 0 ? NSLS : 1];
+    T *sig = a.sig + (size_t)s * 6 * nloc + li;
+    T *mem = a.mem + (size_t)s * 6 * (NSLS > 0 ? NSLS : 1) * nloc + li;
     if (act) {
         ex = e % a.nx;
         ey = (e / a.nx) % a.ny;
@@ -92,6 +100,22 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT) k_element(const StepArgs<T> a)
         vx = vs[u];
         vy = vs[nuni + u];
         vz = vs[2 * nuni + u];
+        lam = ld_stream(a.lam + li);
+        mu = ld_stream(a.mu + li);
+        if constexpr (ANISO) {
+            cA = ld_stream(a.A + li);
+            cB = ld_stream(a.B + li);
+            cC = ld_stream(a.C + li);
+        }
+#pragma unroll
+        for (int c = 0; c < 6; ++c) sg[c] = ld_stream(sig + c * nloc);
+        if constexpr (NSLS > 0) {
+            tau = ld_stream(a.tau + li);
+#pragma unroll
+            for (int c = 0; c < 6; ++c)
+#pragma unroll
+                for (int q = 0; q < NSLS; ++q) m[c][q] = ld_stream(mem + (size_t)(c * NSLS + q) * nloc);
+        }
         T *my = sv + le * 3 * NP;
         my[p] = vx;
         my[NP + p] = vy;
@@ -121,46 +145,32 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT) k_element(const StepArgs<T> a)
             ezy += svy[pz_] * dz;
             ezx += svx[pz_] * dz;
         }
-        // spherical completion (theta = x, phi = y, r = z)
-        const T rr = a.r[ez * P + k];
+        // spherical completion (theta = x, phi = y, r = z); divisions by r and
+        // r*sin(theta) are products with tabulated reciprocals
+        const T rr = a.r[ez * P + k], ir = a.inv_r[ez * P + k];
         const T st = a.sin_t[ex * P + i], ct = a.cot_t[ex * P + i];
-        const T rs = rr * st;
+        const T rs = rr * st, irs = ir * a.inv_sin[ex * P + i];
         ezz = -ezz;
-        eyy = eyy / rs + (vz + vx * ct) / rr;
-        exx = (vz + exx) / rr;
+        eyy = eyy * irs + (vz + vx * ct) * ir;
+        exx = (vz + exx) * ir;
         ezx = -ezx;
-        exz = (exz - vx) / rr;
+        exz = (exz - vx) * ir;
         ezy = -ezy;
-        eyz = -vy / rr + eyz / rs;
-        exy = exy / rr;
-        eyx = -(vy * ct) / rr + eyx / rs;
+        eyz = -vy * ir + eyz * irs;
+        exy = exy * ir;
+        eyx = -(vy * ct) * ir + eyx * irs;
         exy = (exy + eyx) * T(0.5);
         exz = (exz + ezx) * T(0.5);
         eyz = (eyz + ezy) * T(0.5);
 
         // stress rates
-        const size_t li = (size_t)e * NP + p;
-        const T lam = ld_stream(a.lam + li), mu = ld_stream(a.mu + li);
-        T cA = 0, cB = 0, cC = 0;
-        if constexpr (ANISO) {
-            cA = ld_stream(a.A + li);
-            cB = ld_stream(a.B + li);
-            cC = ld_stream(a.C + li);
-        }
+        const T third = T(1) / T(3);
         const T two_mu = T(2) * mu;
         const T tr = exx + eyy + ezz;
         T rxx, ryy, rzz, rxy, rxz, ryz;
-        T *sig = a.sig + (size_t)s * 6 * nloc + li;
         if constexpr (NSLS > 0) {
-            const T tau = ld_stream(a.tau + li);
             const T mu_tau = (T(1) + tau) * mu;
-            const T kappa = lam + two_mu / T(3);
-            T *mem = a.mem + (size_t)s * 6 * NSLS * nloc + li;
-            T m[6][NSLS];
-#pragma unroll
-            for (int c = 0; c < 6; ++c)
-#pragma unroll
-                for (int q = 0; q < NSLS; ++q) m[c][q] = ld_stream(mem + (size_t)(c * NSLS + q) * nloc);
+            const T kappa = lam + two_mu * third;
             T sm[6];
 #pragma unroll
             for (int c = 0; c < 6; ++c) {
@@ -169,26 +179,14 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT) k_element(const StepArgs<T> a)
                 for (int q = 0; q < NSLS; ++q) acc += m[c][q];
                 sm[c] = acc;
             }
-            const T L = (kappa - T(2) * mu_tau / T(3)) * tr - two_mu * (sm[0] + sm[1] + sm[2]) / T(3);
             const T tmt = T(2) * mu_tau;
+            const T L = (kappa - tmt * third) * tr - two_mu * (sm[0] + sm[1] + sm[2]) * third;
             rxx = L + tmt * exx + two_mu * sm[0];
             ryy = L + tmt * eyy + two_mu * sm[1];
             rzz = L + tmt * ezz + two_mu * sm[2];
             rxy = tmt * exy + two_mu * sm[3];
             rxz = tmt * exz + two_mu * sm[4];
             ryz = tmt * eyz + two_mu * sm[5];
-            // memory variables (after the stress update, with this step's rates)
-            const T er[6] = {exx, eyy, ezz, exy, exz, eyz};
-#pragma unroll
-            for (int q = 0; q < NSLS; ++q) {
-                const T tp = a.tau_p[q];
-                const T Lq = a.dt * tau / (T(NSLS) * tp);
-#pragma unroll
-                for (int c = 0; c < 6; ++c) {
-                    const T mv = m[c][q];
-                    st_stream(mem + (size_t)(c * NSLS + q) * nloc, mv - a.dt * mv / tp - Lq * er[c]);
-                }
-            }
         } else {
             const T L = lam * tr;
             rxx = L + two_mu * exx;
@@ -206,19 +204,31 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT) k_element(const StepArgs<T> a)
             ryz += T(2) * cB * eyz;
         }
         // integrate, taper the stored stress
-        const T sxx = ld_stream(sig) + a.dt * rxx;
-        const T sxy = ld_stream(sig + nloc) + a.dt * rxy;
-        const T sxz = ld_stream(sig + 2 * nloc) + a.dt * rxz;
-        const T syy = ld_stream(sig + 3 * nloc) + a.dt * ryy;
-        const T syz = ld_stream(sig + 4 * nloc) + a.dt * ryz;
-        const T szz = ld_stream(sig + 5 * nloc) + a.dt * rzz;
-        const T tp = taper_value(a.px[ex * P + i], a.py[ey * P + j], a.pz[ez * P + k], a.alpha);
+        const T sxx = sg[0] + a.dt * rxx;
+        const T sxy = sg[1] + a.dt * rxy;
+        const T sxz = sg[2] + a.dt * rxz;
+        const T syy = sg[3] + a.dt * ryy;
+        const T syz = sg[4] + a.dt * ryz;
+        const T szz = sg[5] + a.dt * rzz;
+        const T tp = taper_value(a.px[ex * P + i], a.py[ey * P + j], a.pz[ez * P + k], a.inv_alpha);
         st_stream(sig, sxx * tp);
         st_stream(sig + nloc, sxy * tp);
         st_stream(sig + 2 * nloc, sxz * tp);
         st_stream(sig + 3 * nloc, syy * tp);
         st_stream(sig + 4 * nloc, syz * tp);
         st_stream(sig + 5 * nloc, szz * tp);
+        if constexpr (NSLS > 0) {
+            // memory variables after the update, driven by this step's rates:
+            // M <- M*(1 - dt/tau_p) - tau*dt/(n*tau_p)*e
+            const T er[6] = {exx, eyy, ezz, exy, exz, eyz};
+#pragma unroll
+            for (int q = 0; q < NSLS; ++q) {
+                const T drive = tau * a.mem_drive[q];
+#pragma unroll
+                for (int c = 0; c < 6; ++c)
+                    st_stream(mem + (size_t)(c * NSLS + q) * nloc, m[c][q] * a.mem_keep[q] - drive * er[c]);
+            }
+        }
 
         // metric-weighted fluxes for the weak divergence
         const T W = a.w[i] * a.w[j] * a.w[k];
@@ -345,31 +355,39 @@ __global__ void __launch_bounds__(256) k_node(const StepArgs<T> a) {
     const unsigned u = blockIdx.x * 256u + threadIdx.x;
     const int s = blockIdx.y;
     if (u >= (unsigned)a.nuni) return;
+    const size_t nuni = (size_t)a.nuni;
+    T *__restrict__ F = a.F + (size_t)s * 3 * nuni + u;
+    T *__restrict__ v = a.v + (size_t)s * 3 * nuni + u;
+    T *__restrict__ vc = KAHAN ? a.vc + (size_t)s * 3 * nuni + u : nullptr;
+    // all loads before any store (stores to possibly aliasing arrays would
+    // otherwise serialise each thread's later loads behind them)
+    T f[3], vo[3], co[3] = {0, 0, 0};
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        f[c] = F[c * nuni];
+        vo[c] = v[c * nuni];
+        if constexpr (KAHAN) co[c] = vc[c * nuni];
+    }
+    const T im = a.invM[u];
     const unsigned gx = u % (unsigned)a.NXU, rest = u / (unsigned)a.NXU;
     const unsigned gy = rest % (unsigned)a.NYU, gz = rest / (unsigned)a.NYU;
     int ex, i, ey, j, ez, k;
     unique_to_local<N>(gx, a.nx, ex, i);
     unique_to_local<N>(gy, a.ny, ey, j);
     unique_to_local<N>(gz, a.nz, ez, k);
-    const T tp = taper_value(a.px[ex * P + i], a.py[ey * P + j], a.pz[ez * P + k], a.alpha);
-    const T im = a.invM[u];
-    const size_t nuni = (size_t)a.nuni;
+    const T tp = taper_value(a.px[ex * P + i], a.py[ey * P + j], a.pz[ez * P + k], a.inv_alpha);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const size_t idx = ((size_t)s * 3 + c) * nuni + u;
-        const T f = a.F[idx];
-        a.F[idx] = T(0);
-        const T acc = f * im;
+        F[c * nuni] = T(0);
+        const T acc = f[c] * im;
         if constexpr (KAHAN) {
             // Kahan-compensated v += dt*acc (the compensation is tapered with v)
-            const T vold = a.v[idx];
-            const T y = a.dt * acc - a.vc[idx];
-            const T tsum = vold + y;
-            const T comp = (tsum - vold) - y;
-            a.v[idx] = tsum * tp;
-            a.vc[idx] = comp * tp;
+            const T y = a.dt * acc - co[c];
+            const T tsum = vo[c] + y;
+            vc[c * nuni] = ((tsum - vo[c]) - y) * tp;
+            v[c * nuni] = tsum * tp;
         } else {
-            a.v[idx] = (a.v[idx] + a.dt * acc) * tp;
+            v[c * nuni] = (vo[c] + a.dt * acc) * tp;
         }
     }
 }
@@ -490,7 +508,7 @@ __global__ void __launch_bounds__(256) k_taper_local(const StepArgs<T> a, T *loc
     const int p = (int)(li - e * NP);
     const int i = p % P, j = (p / P) % P, k = p / (P * P);
     const int ex = (int)(e % a.nx), ey = (int)((e / a.nx) % a.ny), ez = (int)(e / ((size_t)a.nx * a.ny));
-    loc[li] = taper_value(a.px[ex * P + i], a.py[ey * P + j], a.pz[ez * P + k], a.alpha);
+    loc[li] = taper_value(a.px[ex * P + i], a.py[ey * P + j], a.pz[ez * P + k], a.inv_alpha);
 }
 
 // ---------------------------------------------------------------------------
@@ -500,16 +518,23 @@ template <int N, typename T, int NSLS, bool ANISO>
 int launch_element_v(const StepArgs<T> &a, void *stream) {
     using C = ElemCfg<N>;
     const size_t smem = sizeof(T) * (4 * C::P * C::P + C::EPB * 12 * C::NP);
-    static bool attr_set = false;
-    if (!attr_set) {
-        if (cudaFuncSetAttribute(k_element<N, T, NSLS, ANISO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem) != cudaSuccess)
-            return -1;
-        attr_set = true;
-    }
     const long long blocks = (long long)((a.nel + C::EPB - 1) / C::EPB) * a.S;
     k_element<N, T, NSLS, ANISO><<<(unsigned)blocks, C::NT, smem, (cudaStream_t)stream>>>(a);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+// Opt in to more than 48 KB of dynamic shared memory where a variant needs
+// it (FP64 at high degree). Called once per handle, outside stream capture.
+template <int N, typename T>
+int prepare_element() {
+    using C = ElemCfg<N>;
+    const size_t smem = sizeof(T) * (4 * C::P * C::P + C::EPB * 12 * C::NP);
+    if (smem <= 48 * 1024) return 0;
+    cudaError_t e = cudaFuncSetAttribute(k_element<N, T, 0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_element<N, T, 0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_element<N, T, kNsls, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_element<N, T, kNsls, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return e == cudaSuccess ? 0 : -1;
 }
 
 template <int N, typename T>
@@ -577,7 +602,7 @@ const LpdOps<T> *lpd_ops_n() {
     static const LpdOps<T> ops = {
         &launch_element<N, T>,        &launch_node<N, T>,        &launch_sources<N, T>,
         &launch_receivers<N, T>,      &launch_inv_mass<N, T>,    &launch_gather_local<N, T>,
-        &launch_scatter_unique<N, T>, &launch_taper_local<N, T>, ElemCfg<N>::NT,
+        &launch_scatter_unique<N, T>, &launch_taper_local<N, T>, &prepare_element<N, T>, ElemCfg<N>::NT,
         sizeof(T) * (4 * ElemCfg<N>::P * ElemCfg<N>::P + ElemCfg<N>::EPB * 12 * ElemCfg<N>::NP)};
     return &ops;
 }

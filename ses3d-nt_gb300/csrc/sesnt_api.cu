@@ -139,6 +139,7 @@ struct sesnt_handle {
     size_t dev_bytes = 0;
     // device buffers (typed by precision)
     void *tabD = nullptr, *w = nullptr, *sin_t = nullptr, *cot_t = nullptr, *r = nullptr;
+    void *inv_r = nullptr, *inv_sin = nullptr;
     void *px = nullptr, *py = nullptr, *pz = nullptr;
     double *dsin = nullptr, *dr = nullptr, *dw = nullptr;
     void *lam = nullptr, *mu = nullptr, *A = nullptr, *B = nullptr, *C = nullptr, *tau = nullptr;
@@ -220,7 +221,13 @@ struct sesnt_handle {
         a.nx = g.nx; a.ny = g.ny; a.nz = g.nz; a.nel = nel; a.S = S;
         a.NXU = NXU; a.NYU = NYU; a.NZU = NZU; a.nuni = nuni; a.nloc = nloc;
         a.dt = (T)dt; a.c1 = (T)c1; a.c2 = (T)c2; a.c3 = (T)c3; a.jac = (T)jac; a.alpha = (T)alpha;
-        for (int q = 0; q < kNsls; ++q) a.tau_p[q] = (T)kTauP[q];
+        a.inv_alpha = alpha > 0 ? (T)(1.0 / alpha) : T(0);
+        for (int q = 0; q < kNsls; ++q) {
+            a.tau_p[q] = (T)kTauP[q];
+            a.mem_keep[q] = (T)(1.0 - dt / kTauP[q]);
+            a.mem_drive[q] = (T)(dt / (kNsls * kTauP[q]));
+        }
+        a.inv_r = (const T *)inv_r; a.inv_sin = (const T *)inv_sin;
         a.tabD = (const T *)tabD; a.w = (const T *)w; a.sin_t = (const T *)sin_t; a.cot_t = (const T *)cot_t;
         a.r = (const T *)r; a.px = (const T *)px; a.py = (const T *)py; a.pz = (const T *)pz;
         a.lam = (const T *)lam; a.mu = (const T *)mu; a.A = (const T *)A; a.B = (const T *)B; a.C = (const T *)C;
@@ -302,17 +309,19 @@ int setup_tables(sesnt_t *h) {
     for (int i = 0; i < P; ++i) wt[i] = (T)wd[i];
     std::vector<T> xc = element_coordinates<T>(g.nx, N, d.x_loc_min, d.x_loc_max);
     std::vector<T> zc = element_coordinates<T>(g.nz, N, d.z_loc_max, d.z_loc_min);  // radius decreases with k
-    std::vector<T> st(xc.size()), ct(xc.size()), rr(zc.size());
+    std::vector<T> st(xc.size()), ct(xc.size()), ist(xc.size()), rr(zc.size()), irr(zc.size());
     std::vector<double> dsin(xc.size()), drr(zc.size());
     for (size_t a = 0; a < xc.size(); ++a) {
         const double th = (double)xc[a];
         dsin[a] = std::sin(th);
         st[a] = (T)dsin[a];
         ct[a] = (T)(std::cos(th) / std::sin(th));
+        ist[a] = (T)(1.0 / dsin[a]);
     }
     for (size_t a = 0; a < zc.size(); ++a) {
         drr[a] = (double)zc[a];
         rr[a] = zc[a];
+        irr[a] = (T)(1.0 / drr[a]);
     }
     std::vector<T> pxv, pyv, pzv;
     taper_profiles<T>(g.nx, g.ny, g.nz, N, g.taper_width, (T)g.taper_slope, d, pxv, pyv, pzv);
@@ -322,6 +331,8 @@ int setup_tables(sesnt_t *h) {
     if ((rc = upload(h, h->sin_t, st, "sin"))) return rc;
     if ((rc = upload(h, h->cot_t, ct, "cot"))) return rc;
     if ((rc = upload(h, h->r, rr, "r"))) return rc;
+    if ((rc = upload(h, h->inv_r, irr, "1/r"))) return rc;
+    if ((rc = upload(h, h->inv_sin, ist, "1/sin"))) return rc;
     if ((rc = upload(h, h->px, pxv, "px"))) return rc;
     if ((rc = upload(h, h->py, pyv, "py"))) return rc;
     if ((rc = upload(h, h->pz, pzv, "pz"))) return rc;
@@ -791,6 +802,7 @@ int sesnt_create(const sesnt_grid_t *grid, sesnt_t **out) {
         {&h->tabD, 4 * P * P * E, "tables"}, {&h->w, P * E, "weights"},
         {&h->sin_t, grid->nx * P * E, "sin"}, {&h->cot_t, grid->nx * P * E, "cot"},
         {&h->r, grid->nz * P * E, "r"}, {&h->px, grid->nx * P * E, "px"},
+        {&h->inv_r, grid->nz * P * E, "1/r"}, {&h->inv_sin, grid->nx * P * E, "1/sin"},
         {&h->py, grid->ny * P * E, "py"}, {&h->pz, grid->nz * P * E, "pz"},
         {(void **)&h->dsin, grid->nx * P * 8, "dsin"}, {(void **)&h->dr, grid->nz * P * 8, "dr"},
         {(void **)&h->dw, P * 8, "dw"},
@@ -812,6 +824,10 @@ int sesnt_create(const sesnt_grid_t *grid, sesnt_t **out) {
     if (h->kahan && (rc = h->alloc(&h->vc, 3 * nuni * E * S, "compensation"))) {
         g_create_error = h->err;
         return rc;
+    }
+    if ((h->dbl ? lpd_ops<double>(h->N)->prepare() : lpd_ops<float>(h->N)->prepare()) != 0) {
+        g_create_error = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(cudaGetLastError());
+        return SESNT_ECUDA;
     }
     rc = h->dbl ? setup_tables<double>(h.get()) : setup_tables<float>(h.get());
     if (rc) {

@@ -45,10 +45,13 @@ struct StepArgs {
     int nx, ny, nz, nel, S;
     int NXU, NYU, NZU;
     long long nuni, nloc;
-    T dt, c1, c2, c3, jac, alpha;
+    T dt, c1, c2, c3, jac, alpha, inv_alpha;
     T tau_p[kNsls];
+    T mem_keep[kNsls];   // 1 - dt/tau_p(k)
+    T mem_drive[kNsls];  // dt/(n_sls*tau_p(k))
     // small tables (device): tabD = [Dx | Dy | Dz | Dt], each P*P
     const T *tabD, *w, *sin_t, *cot_t, *r, *px, *py, *pz;
+    const T *inv_r, *inv_sin;  // 1/r [nz*P], 1/sin(theta) [nx*P]
     // model (element-local)
     const T *lam, *mu, *A, *B, *C, *tau;
     // state
@@ -87,6 +90,8 @@ struct LpdOps {
     int (*scatter_unique)(const StepArgs<T> &, const T *loc, T *uni, void *stream);
     // element-local taper (for get_field).
     int (*taper_local)(const StepArgs<T> &, T *loc, void *stream);
+    // one-time kernel attributes (large dynamic shared memory)
+    int (*prepare)();
     int threads_element;
     size_t smem_element;
 };

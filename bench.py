@@ -264,7 +264,7 @@ def run_ours(args):
         line["kernels_ms_per_step"] = {"element": prof[0] / KP, "sources": prof[1] / KP, "node": prof[2] / KP,
                                        "receivers": prof[3] / KP}
         traffic = None
-        tr_path = os.path.join(ROOT, "profiles", "element_kernel_traffic.json")
+        tr_path = os.path.join(ROOT, "profiles", "k_element_%s.traffic.json" % wl.name)
         if os.path.exists(tr_path):
             try:
                 with open(tr_path) as f:

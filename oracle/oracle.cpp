@@ -11,11 +11,15 @@
 // expressions keep the reference's evaluation order (Fortran evaluates left
 // to right; `a**2` is a*a), and the file is compiled with
 // -ffp-contract=off so no multiply-add is fused that the reference would
-// round twice. Parity with the reference for the step itself is anchored on
-// this restatement; the reference ships no seismogram goldens (its only
-// solver-adjacent tests are the GLL, coordinate and interpolation unit
-// programs under src/examples/, whose checks tests/test_oracle_pins.py
-// restates against this file).
+// round twice.
+//
+// Pinned: the GLL tables, coordinates, Lagrange interpolation and assembly
+// map, against the reference's own unit programs under src/examples/
+// (gll_test, coordinates_test, interpolation_test) and its tabulated
+// constants, in tests/test_oracle_pins.py.
+// Parity unpinned for the time step itself: the reference ships no solver
+// tests, seismograms or golden wavefields, and it is Fortran + MPI with no
+// compiler available, so it cannot be run to produce them.
 //
 // The visco-elastic (standard linear solid) branch is commented out in the
 // reference (src/evolution.f90:216-284,415-442). It is restated here from

@@ -207,6 +207,20 @@ int sesnt_v_ptp(sesnt_t *h, int sim, float out[2]);
  * field is float32 in the reference raw layout; in place. Synchronous. */
 int sesnt_assemble_field(sesnt_t *h, float *field);
 
+/* No counterpart in the reference. The same assembly as
+ * sesnt_assemble_field, for callers that cannot allocate device memory at the
+ * time of the call (a stream being captured into a CUDA graph, a time loop
+ * that must not synchronise the device as cudaMalloc/cudaFree do, a host
+ * that reserved all device memory up front). d_in and d_out are device
+ * pointers to float32 fields in the reference raw layout and may be the same
+ * buffer. Nothing is allocated: the unique-point sums use a fixed device
+ * array of 4,194,304 floats (16 MiB) that every GPU loading this library
+ * holds until exit; grids with more unique points get SESNT_ERANGE. The first
+ * call on a device looks up that array's address, so make it before any
+ * stream capture. All calls share the array: calls that overlap on the GPU
+ * race. Runs on the handle's stream and waits for it. */
+int sesnt_assemble_field_noalloc(sesnt_t *h, const float *d_in, float *d_out);
+
 /* Sizes: out[0] elements, out[1] element-local GLL points (N_loc), out[2]
  * unique GLL points (N_uni), out[3] device bytes held by the handle,
  * out[4] algorithmic HBM bytes of one time step (whole batch),

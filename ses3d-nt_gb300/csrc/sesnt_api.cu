@@ -241,6 +241,19 @@ struct sesnt_handle {
     }
 };
 
+namespace sesnt {
+const sesnt_grid *handle_grid(const sesnt_handle *h) { return &h->g; }
+int handle_fail(sesnt_handle *h, int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    h->err = buf;
+    return code;
+}
+}  // namespace sesnt
+
 namespace {
 
 int check_grid(const sesnt_grid_t *g, std::string &why) {

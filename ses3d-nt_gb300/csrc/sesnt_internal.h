@@ -20,7 +20,14 @@
 #include <string>
 #include <vector>
 
+struct sesnt_handle;
+struct sesnt_grid;
+
 namespace sesnt {
+
+// Handle accessors for entry points defined outside sesnt_api.cu.
+const sesnt_grid *handle_grid(const sesnt_handle *h);
+int handle_fail(sesnt_handle *h, int code, const char *fmt, ...);
 
 constexpr int kMaxLpd = 7;
 constexpr int kMinLpd = 2;

@@ -210,6 +210,8 @@ def run_ours(args):
     KP = args.profile_steps
     wl = make_workload(args.workload, W + K + KP + 1)
     g = wl.grid
+    if args.element == "persistent":
+        g.flags |= sesnt.FLAG_PERSISTENT_ELEMENT
     S = g.batch
     hbm, peak_kind = peaks()
 
@@ -249,7 +251,7 @@ def run_ours(args):
                    "algorithmic_bytes_per_step": info["algorithmic_bytes_per_step"],
                    "l2": "inputs larger than L2 (%.2f GB touched per step vs 0.13 GB L2)"
                          % (info["algorithmic_bytes_per_step"] / 1e9),
-                   "graph": not (g.flags & sesnt.FLAG_NO_GRAPH),
+                   "graph": not (g.flags & sesnt.FLAG_NO_GRAPH), "element_kernel": args.element,
                    "parallelism": "replicas" if WORLD > 1 else "single GPU"},
         "gpu_launches": int(K * info["launches_per_step"] + math.ceil(K / 32.0) + 1),
         "clocks": clk,
@@ -375,6 +377,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-seconds", type=float, default=60.0)
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
+    ap.add_argument("--element", default="simple", choices=["persistent", "simple"],
+                    help="element kernel variant (both compute the full step)")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")

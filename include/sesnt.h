@@ -48,6 +48,8 @@ extern "C" {
 /* flags (sesnt_grid_t.flags) */
 #define SESNT_FLAG_KAHAN 1u      /* compensated velocity update */
 #define SESNT_FLAG_NO_GRAPH 2u   /* sesnt_run launches kernels directly, no CUDA graph */
+#define SESNT_FLAG_PERSISTENT_ELEMENT 4u /* persistent element kernel that prefetches the next
+                                            element groups with cp.async (same results) */
 
 /* source kinds (sesnt_add_source) */
 #define SESNT_SOURCE_MT 0 /* moment tensor: comp = Mxx Mxy Mxz Myy Myz Mzz */

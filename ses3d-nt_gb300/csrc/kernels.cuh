@@ -26,28 +26,58 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "sesnt_internal.h"
 
 namespace sesnt {
+
+// Launch shape of the element kernel, chosen by measurement on GB300 (config-2
+// workload, lpd 4, 3 SLS): one element per 128-thread block with registers
+// sized for 8 resident blocks beat 2 or 4 elements per block by 7-10%.
+#ifndef SESNT_EPB_LPD4
+#define SESNT_EPB_LPD4 1
+#endif
+#ifndef SESNT_MINB_256
+#define SESNT_MINB_256 4
+#endif
 
 template <int N>
 struct ElemCfg {
     static constexpr int P = N + 1;
     static constexpr int NP = P * P * P;
     // elements per block: enough points to fill whole warps with little waste
-    static constexpr int EPB = NP <= 32 ? 8 : (NP <= 64 ? 2 : (NP <= 128 ? 2 : 1));
+    static constexpr int EPB = N == 4 ? SESNT_EPB_LPD4 : (NP <= 32 ? 8 : (NP <= 64 ? 2 : (NP <= 128 ? 2 : 1)));
     static constexpr int NT = ((EPB * NP + 31) / 32) * 32;
     // resident blocks per SM the register allocation is sized for
-    static constexpr int MINB = NT <= 256 ? 4 : (NT <= 384 ? 2 : 1);
+    static constexpr int MINB = NT <= 128 ? 2 * SESNT_MINB_256 : (NT <= 256 ? SESNT_MINB_256 : (NT <= 512 ? SESNT_MINB_256 / 2 : 1));
 };
 
+// Evict-first hints: measured faster on the stores only (loads without the
+// hint keep the next blocks' shared velocity lines warm).
+#ifndef SESNT_HINT_LOADS
+#define SESNT_HINT_LOADS 0
+#endif
+#ifndef SESNT_HINT_STORES
+#define SESNT_HINT_STORES 1
+#endif
+// Streamed element-local data (stress, memory variables, material) with or
+// without the evict-first cache hint.
 template <typename T>
 __device__ __forceinline__ T ld_stream(const T *p) {
+#if SESNT_HINT_LOADS
     return __ldcs(p);
+#else
+    return *p;
+#endif
 }
 template <typename T>
 __device__ __forceinline__ void st_stream(T *p, T v) {
+#if SESNT_HINT_STORES
     __stcs(p, v);
+#else
+    *p = v;
+#endif
 }
 
 // Taper from the three damping profiles (src/geometric_paras.f90:308-316):
@@ -61,9 +91,167 @@ __device__ __forceinline__ T taper_value(T px, T py, T pz, T inv_alpha) {
     return exp(-(T(0.1) * (p2 * p2)));
 }
 
+// One element-local point of the step, from the velocity slab in shared
+// memory and the point's own stress, memory variables and material: velocity
+// gradient (line contractions), spherical completion, stress rate (elastic or
+// standard linear solids, optional A,B,C), integration, taper of the stored
+// stress, memory-variable update, and the metric-weighted stresses of the
+// weak divergence written to the flux slab `my`.
+template <int N, typename T, int NSLS, bool ANISO>
+__device__ __forceinline__ void point_step(const StepArgs<T> &a, const T *sD, const T *svx, const T *svy,
+                                           const T *svz, int p, int i, int j, int k, int ex, int ey, int ez,
+                                           T lam, T mu, T tau, T cA, T cB, T cC, const T (&sg)[6],
+                                           const T (&m)[6][NSLS > 0 ? NSLS : 1], T *sig, T *mem, size_t nloc,
+                                           T *my) {
+    constexpr int P = N + 1, NP = P * P * P;
+    const T *Dx = sD, *Dy = sD + P * P, *Dz = sD + 2 * P * P;
+    const T vx = svx[p], vy = svy[p], vz = svz[p];
+    // velocity gradient: line contractions along the three GLL directions
+    T exx = 0, exy = 0, exz = 0, eyy = 0, eyx = 0, eyz = 0, ezz = 0, ezy = 0, ezx = 0;
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+        const int px_ = q + P * (j + P * k);
+        const int py_ = i + P * (q + P * k);
+        const int pz_ = i + P * (j + P * q);
+        const T dx = Dx[q * P + i], dy = Dy[q * P + j], dz = Dz[q * P + k];
+        exx += svx[px_] * dx;
+        exy += svy[px_] * dx;
+        exz += svz[px_] * dx;
+        eyy += svy[py_] * dy;
+        eyx += svx[py_] * dy;
+        eyz += svz[py_] * dy;
+        ezz += svz[pz_] * dz;
+        ezy += svy[pz_] * dz;
+        ezx += svx[pz_] * dz;
+    }
+    // spherical completion (theta = x, phi = y, r = z); divisions by r and
+    // r*sin(theta) are products with tabulated reciprocals
+    const T rr = a.r[ez * P + k], ir = a.inv_r[ez * P + k];
+    const T st = a.sin_t[ex * P + i], ct = a.cot_t[ex * P + i];
+    const T rs = rr * st, irs = ir * a.inv_sin[ex * P + i];
+    ezz = -ezz;
+    eyy = eyy * irs + (vz + vx * ct) * ir;
+    exx = (vz + exx) * ir;
+    ezx = -ezx;
+    exz = (exz - vx) * ir;
+    ezy = -ezy;
+    eyz = -vy * ir + eyz * irs;
+    exy = exy * ir;
+    eyx = -(vy * ct) * ir + eyx * irs;
+    exy = (exy + eyx) * T(0.5);
+    exz = (exz + ezx) * T(0.5);
+    eyz = (eyz + ezy) * T(0.5);
+
+    // stress rates
+    const T third = T(1) / T(3);
+    const T two_mu = T(2) * mu;
+    const T tr = exx + eyy + ezz;
+    T rxx, ryy, rzz, rxy, rxz, ryz;
+    if constexpr (NSLS > 0) {
+        const T mu_tau = (T(1) + tau) * mu;
+        const T kappa = lam + two_mu * third;
+        T sm[6];
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            T acc = 0;
+#pragma unroll
+            for (int q = 0; q < NSLS; ++q) acc += m[c][q];
+            sm[c] = acc;
+        }
+        const T tmt = T(2) * mu_tau;
+        const T L = (kappa - tmt * third) * tr - two_mu * (sm[0] + sm[1] + sm[2]) * third;
+        rxx = L + tmt * exx + two_mu * sm[0];
+        ryy = L + tmt * eyy + two_mu * sm[1];
+        rzz = L + tmt * ezz + two_mu * sm[2];
+        rxy = tmt * exy + two_mu * sm[3];
+        rxz = tmt * exz + two_mu * sm[4];
+        ryz = tmt * eyz + two_mu * sm[5];
+    } else {
+        const T L = lam * tr;
+        rxx = L + two_mu * exx;
+        ryy = L + two_mu * eyy;
+        rzz = L + two_mu * ezz;
+        rxy = two_mu * exy;
+        rxz = two_mu * exz;
+        ryz = two_mu * eyz;
+    }
+    if constexpr (ANISO) {
+        rxx += cC * ezz + cA * (eyy + exx);
+        ryy += cC * ezz + cA * (eyy + exx);
+        rzz += cC * (eyy + exx);
+        rxz += T(2) * cB * exz;
+        ryz += T(2) * cB * eyz;
+    }
+    // integrate, taper the stored stress
+    const T sxx = sg[0] + a.dt * rxx;
+    const T sxy = sg[1] + a.dt * rxy;
+    const T sxz = sg[2] + a.dt * rxz;
+    const T syy = sg[3] + a.dt * ryy;
+    const T syz = sg[4] + a.dt * ryz;
+    const T szz = sg[5] + a.dt * rzz;
+    const T tp = taper_value(a.px[ex * P + i], a.py[ey * P + j], a.pz[ez * P + k], a.inv_alpha);
+    st_stream(sig, sxx * tp);
+    st_stream(sig + nloc, sxy * tp);
+    st_stream(sig + 2 * nloc, sxz * tp);
+    st_stream(sig + 3 * nloc, syy * tp);
+    st_stream(sig + 4 * nloc, syz * tp);
+    st_stream(sig + 5 * nloc, szz * tp);
+    if constexpr (NSLS > 0) {
+        // memory variables after the update, driven by this step's rates:
+        // M <- M*(1 - dt/tau_p) - tau*dt/(n*tau_p)*e
+        const T er[6] = {exx, eyy, ezz, exy, exz, eyz};
+#pragma unroll
+        for (int q = 0; q < NSLS; ++q) {
+            const T drive = tau * a.mem_drive[q];
+#pragma unroll
+            for (int c = 0; c < 6; ++c)
+                st_stream(mem + (size_t)(c * NSLS + q) * nloc, m[c][q] * a.mem_keep[q] - drive * er[c]);
+        }
+    }
+    // metric-weighted stresses for the weak divergence
+    const T W = a.w[i] * a.w[j] * a.w[k];
+    const T gx = W * rs * a.c1;
+    const T gy = W * rr * a.c2;
+    const T gz = W * (rr * rs) * a.c3;
+    my[0 * NP + p] = sxx * gx;
+    my[1 * NP + p] = sxy * gy;
+    my[2 * NP + p] = sxz * gz;
+    my[3 * NP + p] = sxy * gx;
+    my[4 * NP + p] = syy * gy;
+    my[5 * NP + p] = syz * gz;
+    my[6 * NP + p] = sxz * gx;
+    my[7 * NP + p] = syz * gy;
+    my[8 * NP + p] = szz * gz;
+}
+
+// Weak divergence at point (i,j,k): transposed line contractions over the
+// element's flux slab `my` (9 x NP).
+template <int N, typename T>
+__device__ __forceinline__ void point_divergence(const T *Dt, const T *my, int i, int j, int k, T &fx, T &fy,
+                                                 T &fz) {
+    constexpr int P = N + 1, NP = P * P * P;
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+        const int px_ = q + P * (j + P * k);
+        const int py_ = i + P * (q + P * k);
+        const int pz_ = i + P * (j + P * q);
+        const T di = Dt[i * P + q], dj = Dt[j * P + q], dk = Dt[k * P + q];
+        fx += my[2 * NP + pz_] * dk + my[1 * NP + py_] * dj + my[0 * NP + px_] * di;
+        fy += my[5 * NP + pz_] * dk + my[4 * NP + py_] * dj + my[3 * NP + px_] * di;
+        fz += my[8 * NP + pz_] * dk + my[7 * NP + py_] * dj + my[6 * NP + px_] * di;
+    }
+}
+
+template <int N>
+__device__ __forceinline__ size_t unique_index(int NXU, int NYU, int ex, int ey, int ez, int i, int j, int k) {
+    return (size_t)(ex * N + i) + (size_t)NXU * ((size_t)(ey * N + j) + (size_t)NYU * (size_t)(ez * N + k));
+}
+
+// One block per group of EPB elements and simulation.
 template <int N, typename T, int NSLS, bool ANISO>
 __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::MINB : 1) k_element(const StepArgs<T> a) {
     constexpr int P = ElemCfg<N>::P, NP = ElemCfg<N>::NP, EPB = ElemCfg<N>::EPB, NT = ElemCfg<N>::NT;
+    constexpr int MS = NSLS > 0 ? NSLS : 1;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *sD = reinterpret_cast<T *>(smem_raw);  // [4][P*P]
     T *sv = sD + 4 * P * P;                   // [EPB][3][NP]
@@ -85,21 +273,19 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::M
     const size_t nuni = (size_t)a.nuni, nloc = (size_t)a.nloc;
     const size_t li = (size_t)e * NP + p;
     // Every global load of the step is issued here, before any store, so the
-    // loads overlap each other and the line contractions below.
-    T vx = 0, vy = 0, vz = 0, lam = 0, mu = 0, tau = 0, cA = 0, cB = 0, cC = 0;
+    // loads overlap each other and the line contractions.
+    T lam = 0, mu = 0, tau = 0, cA = 0, cB = 0, cC = 0;
     T sg[6] = {0, 0, 0, 0, 0, 0};
-    T m[NSLS > 0 ? 6 : 1][NSLS > 0 ? NSLS : 1];
+    T m[6][MS];
     T *sig = a.sig + (size_t)s * 6 * nloc + li;
-    T *mem = a.mem + (size_t)s * 6 * (NSLS > 0 ? NSLS : 1) * nloc + li;
+    T *mem = a.mem + (size_t)s * 6 * MS * nloc + li;
     if (act) {
         ex = e % a.nx;
         ey = (e / a.nx) % a.ny;
         ez = e / (a.nx * a.ny);
-        u = (size_t)(ex * N + i) + (size_t)a.NXU * ((size_t)(ey * N + j) + (size_t)a.NYU * (size_t)(ez * N + k));
+        u = unique_index<N>(a.NXU, a.NYU, ex, ey, ez, i, j, k);
         const T *vs = a.v + (size_t)s * 3 * nuni;
-        vx = vs[u];
-        vy = vs[nuni + u];
-        vz = vs[2 * nuni + u];
+        const T vx = vs[u], vy = vs[nuni + u], vz = vs[2 * nuni + u];
         lam = ld_stream(a.lam + li);
         mu = ld_stream(a.mu + li);
         if constexpr (ANISO) {
@@ -122,149 +308,188 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::M
         my[2 * NP + p] = vz;
     }
     __syncthreads();
-
-    T fx = 0, fy = 0, fz = 0;
     if (act) {
-        const T *Dx = sD, *Dy = sD + P * P, *Dz = sD + 2 * P * P;
-        const T *svx = sv + le * 3 * NP, *svy = svx + NP, *svz = svx + 2 * NP;
-        // velocity gradient: line contractions along the three GLL directions
-        T exx = 0, exy = 0, exz = 0, eyy = 0, eyx = 0, eyz = 0, ezz = 0, ezy = 0, ezx = 0;
-#pragma unroll
-        for (int q = 0; q < P; ++q) {
-            const int px_ = q + P * (j + P * k);
-            const int py_ = i + P * (q + P * k);
-            const int pz_ = i + P * (j + P * q);
-            const T dx = Dx[q * P + i], dy = Dy[q * P + j], dz = Dz[q * P + k];
-            exx += svx[px_] * dx;
-            exy += svy[px_] * dx;
-            exz += svz[px_] * dx;
-            eyy += svy[py_] * dy;
-            eyx += svx[py_] * dy;
-            eyz += svz[py_] * dy;
-            ezz += svz[pz_] * dz;
-            ezy += svy[pz_] * dz;
-            ezx += svx[pz_] * dz;
-        }
-        // spherical completion (theta = x, phi = y, r = z); divisions by r and
-        // r*sin(theta) are products with tabulated reciprocals
-        const T rr = a.r[ez * P + k], ir = a.inv_r[ez * P + k];
-        const T st = a.sin_t[ex * P + i], ct = a.cot_t[ex * P + i];
-        const T rs = rr * st, irs = ir * a.inv_sin[ex * P + i];
-        ezz = -ezz;
-        eyy = eyy * irs + (vz + vx * ct) * ir;
-        exx = (vz + exx) * ir;
-        ezx = -ezx;
-        exz = (exz - vx) * ir;
-        ezy = -ezy;
-        eyz = -vy * ir + eyz * irs;
-        exy = exy * ir;
-        eyx = -(vy * ct) * ir + eyx * irs;
-        exy = (exy + eyx) * T(0.5);
-        exz = (exz + ezx) * T(0.5);
-        eyz = (eyz + ezy) * T(0.5);
-
-        // stress rates
-        const T third = T(1) / T(3);
-        const T two_mu = T(2) * mu;
-        const T tr = exx + eyy + ezz;
-        T rxx, ryy, rzz, rxy, rxz, ryz;
-        if constexpr (NSLS > 0) {
-            const T mu_tau = (T(1) + tau) * mu;
-            const T kappa = lam + two_mu * third;
-            T sm[6];
-#pragma unroll
-            for (int c = 0; c < 6; ++c) {
-                T acc = 0;
-#pragma unroll
-                for (int q = 0; q < NSLS; ++q) acc += m[c][q];
-                sm[c] = acc;
-            }
-            const T tmt = T(2) * mu_tau;
-            const T L = (kappa - tmt * third) * tr - two_mu * (sm[0] + sm[1] + sm[2]) * third;
-            rxx = L + tmt * exx + two_mu * sm[0];
-            ryy = L + tmt * eyy + two_mu * sm[1];
-            rzz = L + tmt * ezz + two_mu * sm[2];
-            rxy = tmt * exy + two_mu * sm[3];
-            rxz = tmt * exz + two_mu * sm[4];
-            ryz = tmt * eyz + two_mu * sm[5];
-        } else {
-            const T L = lam * tr;
-            rxx = L + two_mu * exx;
-            ryy = L + two_mu * eyy;
-            rzz = L + two_mu * ezz;
-            rxy = two_mu * exy;
-            rxz = two_mu * exz;
-            ryz = two_mu * eyz;
-        }
-        if constexpr (ANISO) {
-            rxx += cC * ezz + cA * (eyy + exx);
-            ryy += cC * ezz + cA * (eyy + exx);
-            rzz += cC * (eyy + exx);
-            rxz += T(2) * cB * exz;
-            ryz += T(2) * cB * eyz;
-        }
-        // integrate, taper the stored stress
-        const T sxx = sg[0] + a.dt * rxx;
-        const T sxy = sg[1] + a.dt * rxy;
-        const T sxz = sg[2] + a.dt * rxz;
-        const T syy = sg[3] + a.dt * ryy;
-        const T syz = sg[4] + a.dt * ryz;
-        const T szz = sg[5] + a.dt * rzz;
-        const T tp = taper_value(a.px[ex * P + i], a.py[ey * P + j], a.pz[ez * P + k], a.inv_alpha);
-        st_stream(sig, sxx * tp);
-        st_stream(sig + nloc, sxy * tp);
-        st_stream(sig + 2 * nloc, sxz * tp);
-        st_stream(sig + 3 * nloc, syy * tp);
-        st_stream(sig + 4 * nloc, syz * tp);
-        st_stream(sig + 5 * nloc, szz * tp);
-        if constexpr (NSLS > 0) {
-            // memory variables after the update, driven by this step's rates:
-            // M <- M*(1 - dt/tau_p) - tau*dt/(n*tau_p)*e
-            const T er[6] = {exx, eyy, ezz, exy, exz, eyz};
-#pragma unroll
-            for (int q = 0; q < NSLS; ++q) {
-                const T drive = tau * a.mem_drive[q];
-#pragma unroll
-                for (int c = 0; c < 6; ++c)
-                    st_stream(mem + (size_t)(c * NSLS + q) * nloc, m[c][q] * a.mem_keep[q] - drive * er[c]);
-            }
-        }
-
-        // metric-weighted fluxes for the weak divergence
-        const T W = a.w[i] * a.w[j] * a.w[k];
-        const T gx = W * rs * a.c1;
-        const T gy = W * rr * a.c2;
-        const T gz = W * (rr * rs) * a.c3;
-        T *my = sf + le * 9 * NP;
-        my[0 * NP + p] = sxx * gx;
-        my[1 * NP + p] = sxy * gy;
-        my[2 * NP + p] = sxz * gz;
-        my[3 * NP + p] = sxy * gx;
-        my[4 * NP + p] = syy * gy;
-        my[5 * NP + p] = syz * gz;
-        my[6 * NP + p] = sxz * gx;
-        my[7 * NP + p] = syz * gy;
-        my[8 * NP + p] = szz * gz;
+        const T *svx = sv + le * 3 * NP;
+        point_step<N, T, NSLS, ANISO>(a, sD, svx, svx + NP, svx + 2 * NP, p, i, j, k, ex, ey, ez, lam, mu, tau, cA,
+                                      cB, cC, sg, m, sig, mem, nloc, sf + le * 9 * NP);
     }
     __syncthreads();
     if (act) {
-        const T *Dt = sD + 3 * P * P;
-        const T *my = sf + le * 9 * NP;
-#pragma unroll
-        for (int q = 0; q < P; ++q) {
-            const int px_ = q + P * (j + P * k);
-            const int py_ = i + P * (q + P * k);
-            const int pz_ = i + P * (j + P * q);
-            const T di = Dt[i * P + q], dj = Dt[j * P + q], dk = Dt[k * P + q];
-            fx += my[2 * NP + pz_] * dk + my[1 * NP + py_] * dj + my[0 * NP + px_] * di;
-            fy += my[5 * NP + pz_] * dk + my[4 * NP + py_] * dj + my[3 * NP + px_] * di;
-            fz += my[8 * NP + pz_] * dk + my[7 * NP + py_] * dj + my[6 * NP + px_] * di;
-        }
+        T fx = 0, fy = 0, fz = 0;
+        point_divergence<N, T>(sD + 3 * P * P, sf + le * 9 * NP, i, j, k, fx, fy, fz);
         T *F = a.F + (size_t)s * 3 * nuni;
         atomicAdd(F + u, fx);
         atomicAdd(F + nuni + u, fy);
         atomicAdd(F + 2 * nuni + u, fz);
     }
+}
+
+// ---------------------------------------------------------------------------
+// Persistent variant: each block walks element groups (g, s) with a stride of
+// the grid and stages the next groups' streamed data (stress, memory
+// variables, material) and velocity gather in shared memory with cp.async
+// while it computes the current one (double buffer), so every SM keeps loads
+// in flight through the compute and store phases.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long evict_first_policy() {
+    unsigned long long pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+template <typename T>
+__device__ __forceinline__ void cp_async_stream(T *smem, const T *gmem, unsigned long long pol) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    if constexpr (sizeof(T) == 4)
+        asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 4, %2;" ::"r"(s), "l"(gmem), "l"(pol)
+                     : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 8, %2;" ::"r"(s), "l"(gmem), "l"(pol)
+                     : "memory");
+}
+
+template <typename T>
+__device__ __forceinline__ void cp_async_keep(T *smem, const T *gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    if constexpr (sizeof(T) == 4)
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+template <int K>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(K) : "memory");
+}
+
+template <int N, typename T, int NSLS, bool ANISO>
+struct PfCfg {
+    static constexpr int NP = ElemCfg<N>::NP, EPB = ElemCfg<N>::EPB;
+    // streamed components: 6 stress, 6*NSLS memory, lambda, mu, [tau], [A,B,C]
+    static constexpr int NC = 6 + 6 * NSLS + 2 + (NSLS > 0 ? 1 : 0) + (ANISO ? 3 : 0);
+    static constexpr int SLAB = EPB * NP;
+    static constexpr size_t SMEM =
+        sizeof(T) * (4 * ElemCfg<N>::P * ElemCfg<N>::P + 2 * NC * SLAB + 2 * 3 * SLAB + 9 * SLAB);
+};
+
+template <int N, typename T, int NSLS, bool ANISO>
+__global__ void __launch_bounds__(ElemCfg<N>::NT) k_element_pf(const StepArgs<T> a) {
+    using C = PfCfg<N, T, NSLS, ANISO>;
+    constexpr int P = ElemCfg<N>::P, NP = ElemCfg<N>::NP, EPB = ElemCfg<N>::EPB, NT = ElemCfg<N>::NT;
+    constexpr int MS = NSLS > 0 ? NSLS : 1, NC = C::NC, SLAB = C::SLAB;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sD = reinterpret_cast<T *>(smem_raw);  // [4][P*P]
+    T *stage = sD + 4 * P * P;                // [2][NC][SLAB]
+    T *svb = stage + 2 * NC * SLAB;           // [2][3][SLAB]
+    T *sf = svb + 2 * 3 * SLAB;               // [9][SLAB] (element le at offset le*9*NP)
+
+    const int t = threadIdx.x;
+    for (int x = t; x < 4 * P * P; x += NT) sD[x] = a.tabD[x];
+    const int le = t / NP;
+    const int p = t - le * NP;
+    const int i = p % P, j = (p / P) % P, k = p / (P * P);
+    const int o = le * NP + p;  // this thread's slot in a slab
+    const size_t nuni = (size_t)a.nuni, nloc = (size_t)a.nloc;
+    const int S = a.S;
+    const long long ngroups = (long long)((a.nel + EPB - 1) / EPB) * S;
+    const unsigned long long pol = evict_first_policy();
+
+    auto prefetch = [&](int buf, long long idx) {
+        const int s = (int)(idx % S);
+        const int e = (int)(idx / S) * EPB + le;
+        if (le < EPB && e < a.nel) {
+            const size_t li = (size_t)e * NP + p;
+            T *st = stage + buf * NC * SLAB + o;
+            const T *sig = a.sig + (size_t)s * 6 * nloc + li;
+#pragma unroll
+            for (int c = 0; c < 6; ++c) cp_async_stream(st + c * SLAB, sig + c * nloc, pol);
+            if constexpr (NSLS > 0) {
+                const T *mem = a.mem + (size_t)s * 6 * NSLS * nloc + li;
+#pragma unroll
+                for (int c = 0; c < 6 * NSLS; ++c) cp_async_stream(st + (6 + c) * SLAB, mem + c * nloc, pol);
+            }
+            constexpr int b0 = 6 + 6 * NSLS;
+            cp_async_stream(st + b0 * SLAB, a.lam + li, pol);
+            cp_async_stream(st + (b0 + 1) * SLAB, a.mu + li, pol);
+            if constexpr (NSLS > 0) cp_async_stream(st + (b0 + 2) * SLAB, a.tau + li, pol);
+            if constexpr (ANISO) {
+                constexpr int b1 = b0 + 2 + (NSLS > 0 ? 1 : 0);
+                cp_async_stream(st + b1 * SLAB, a.A + li, pol);
+                cp_async_stream(st + (b1 + 1) * SLAB, a.B + li, pol);
+                cp_async_stream(st + (b1 + 2) * SLAB, a.C + li, pol);
+            }
+            const int ex = e % a.nx, ey = (e / a.nx) % a.ny, ez = e / (a.nx * a.ny);
+            const size_t u = unique_index<N>(a.NXU, a.NYU, ex, ey, ez, i, j, k);
+            const T *vs = a.v + (size_t)s * 3 * nuni + u;
+            T *sv = svb + buf * 3 * SLAB + o;
+            cp_async_keep(sv, vs);
+            cp_async_keep(sv + SLAB, vs + nuni);
+            cp_async_keep(sv + 2 * SLAB, vs + 2 * nuni);
+        }
+        cp_async_commit();
+    };
+
+    long long idx = blockIdx.x;
+    const long long stride = gridDim.x;
+    if (idx < ngroups) prefetch(0, idx);
+    else cp_async_commit();
+    if (idx + stride < ngroups) prefetch(1, idx + stride);
+    else cp_async_commit();
+    for (int it = 0; idx < ngroups; idx += stride, ++it) {
+        const int b = it & 1;
+        const int s = (int)(idx % S);
+        const int e = (int)(idx / S) * EPB + le;
+        const bool act = (le < EPB) && (e < a.nel);
+        cp_async_wait<1>();  // this group's copies have landed (the next group's may still fly)
+        __syncthreads();     // ... and are visible to the whole block
+        int ex = 0, ey = 0, ez = 0;
+        size_t u = 0;
+        if (act) {
+            ex = e % a.nx;
+            ey = (e / a.nx) % a.ny;
+            ez = e / (a.nx * a.ny);
+            u = unique_index<N>(a.NXU, a.NYU, ex, ey, ez, i, j, k);
+            const T *st = stage + b * NC * SLAB + o;
+            T sg[6], m[6][MS];
+#pragma unroll
+            for (int c = 0; c < 6; ++c) sg[c] = st[c * SLAB];
+            if constexpr (NSLS > 0) {
+#pragma unroll
+                for (int c = 0; c < 6; ++c)
+#pragma unroll
+                    for (int q = 0; q < NSLS; ++q) m[c][q] = st[(6 + c * NSLS + q) * SLAB];
+            }
+            constexpr int b0 = 6 + 6 * NSLS;
+            const T lam = st[b0 * SLAB], mu = st[(b0 + 1) * SLAB];
+            T tau = 0, cA = 0, cB = 0, cC = 0;
+            if constexpr (NSLS > 0) tau = st[(b0 + 2) * SLAB];
+            if constexpr (ANISO) {
+                constexpr int b1 = b0 + 2 + (NSLS > 0 ? 1 : 0);
+                cA = st[b1 * SLAB];
+                cB = st[(b1 + 1) * SLAB];
+                cC = st[(b1 + 2) * SLAB];
+            }
+            const size_t li = (size_t)e * NP + p;
+            const T *svx = svb + b * 3 * SLAB + le * NP;
+            point_step<N, T, NSLS, ANISO>(a, sD, svx, svx + SLAB, svx + 2 * SLAB, p, i, j, k, ex, ey, ez, lam, mu,
+                                          tau, cA, cB, cC, sg, m, a.sig + (size_t)s * 6 * nloc + li,
+                                          a.mem + (size_t)s * 6 * MS * nloc + li, nloc, sf + le * 9 * NP);
+        }
+        __syncthreads();  // fluxes complete; buffer b free for the group after next
+        if (idx + 2 * stride < ngroups) prefetch(b, idx + 2 * stride);
+        else cp_async_commit();
+        if (act) {
+            T fx = 0, fy = 0, fz = 0;
+            point_divergence<N, T>(sD + 3 * P * P, sf + le * 9 * NP, i, j, k, fx, fy, fz);
+            T *F = a.F + (size_t)s * 3 * nuni;
+            atomicAdd(F + u, fx);
+            atomicAdd(F + nuni + u, fy);
+            atomicAdd(F + 2 * nuni + u, fz);
+        }
+    }
+    cp_async_wait<0>();
 }
 
 // Source slabs through the weak divergence, one block per resolved
@@ -514,27 +739,69 @@ __global__ void __launch_bounds__(256) k_taper_local(const StepArgs<T> a, T *loc
 // ---------------------------------------------------------------------------
 // Launchers
 // ---------------------------------------------------------------------------
+constexpr size_t kMaxSmemPerBlock = 227 * 1024;
+
+// Resident blocks per SM and SM count for the persistent variant, filled in
+// by prepare_element (outside stream capture).
+template <int N, typename T, int NSLS, bool ANISO>
+struct PfLaunch {
+    static int blocks_per_sm;
+    static int sms;
+};
+template <int N, typename T, int NSLS, bool ANISO>
+int PfLaunch<N, T, NSLS, ANISO>::blocks_per_sm = 0;
+template <int N, typename T, int NSLS, bool ANISO>
+int PfLaunch<N, T, NSLS, ANISO>::sms = 0;
+
 template <int N, typename T, int NSLS, bool ANISO>
 int launch_element_v(const StepArgs<T> &a, void *stream) {
     using C = ElemCfg<N>;
-    const size_t smem = sizeof(T) * (4 * C::P * C::P + C::EPB * 12 * C::NP);
-    const long long blocks = (long long)((a.nel + C::EPB - 1) / C::EPB) * a.S;
-    k_element<N, T, NSLS, ANISO><<<(unsigned)blocks, C::NT, smem, (cudaStream_t)stream>>>(a);
+    using PF = PfCfg<N, T, NSLS, ANISO>;
+    using L = PfLaunch<N, T, NSLS, ANISO>;
+    const long long groups = (long long)((a.nel + C::EPB - 1) / C::EPB) * a.S;
+    if (a.persistent && PF::SMEM <= kMaxSmemPerBlock && L::blocks_per_sm > 0) {
+        const long long blocks = std::min<long long>(groups, (long long)L::blocks_per_sm * L::sms);
+        k_element_pf<N, T, NSLS, ANISO><<<(unsigned)blocks, C::NT, PF::SMEM, (cudaStream_t)stream>>>(a);
+    } else {
+        const size_t smem = sizeof(T) * (4 * C::P * C::P + C::EPB * 12 * C::NP);
+        k_element<N, T, NSLS, ANISO><<<(unsigned)groups, C::NT, smem, (cudaStream_t)stream>>>(a);
+    }
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
-// Opt in to more than 48 KB of dynamic shared memory where a variant needs
-// it (FP64 at high degree). Called once per handle, outside stream capture.
+template <int N, typename T, int NSLS, bool ANISO>
+int prepare_variant() {
+    using C = ElemCfg<N>;
+    using PF = PfCfg<N, T, NSLS, ANISO>;
+    using L = PfLaunch<N, T, NSLS, ANISO>;
+    const size_t smem = sizeof(T) * (4 * C::P * C::P + C::EPB * 12 * C::NP);
+    cudaError_t e = cudaSuccess;
+    if (smem > 48 * 1024)
+        e = cudaFuncSetAttribute(k_element<N, T, NSLS, ANISO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess && PF::SMEM <= kMaxSmemPerBlock) {
+        e = cudaFuncSetAttribute(k_element_pf<N, T, NSLS, ANISO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)PF::SMEM);
+        int dev = 0, nb = 0, sms = 0;
+        if (e == cudaSuccess) e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_element_pf<N, T, NSLS, ANISO>, C::NT, PF::SMEM);
+        if (e == cudaSuccess) {
+            L::blocks_per_sm = nb;
+            L::sms = sms;
+        }
+    }
+    return e == cudaSuccess ? 0 : -1;
+}
+
+// Kernel attributes (large dynamic shared memory) and the persistent grid
+// size, once per handle, outside stream capture.
 template <int N, typename T>
 int prepare_element() {
-    using C = ElemCfg<N>;
-    const size_t smem = sizeof(T) * (4 * C::P * C::P + C::EPB * 12 * C::NP);
-    if (smem <= 48 * 1024) return 0;
-    cudaError_t e = cudaFuncSetAttribute(k_element<N, T, 0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_element<N, T, 0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_element<N, T, kNsls, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_element<N, T, kNsls, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    return e == cudaSuccess ? 0 : -1;
+    if (prepare_variant<N, T, 0, false>() || prepare_variant<N, T, 0, true>() ||
+        prepare_variant<N, T, kNsls, false>() || prepare_variant<N, T, kNsls, true>())
+        return -1;
+    return 0;
 }
 
 template <int N, typename T>

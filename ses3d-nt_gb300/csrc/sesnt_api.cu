@@ -237,6 +237,7 @@ struct sesnt_handle {
         a.src_data = (const T *)d_src_data;
         a.nrec = nrec_dev; a.rec_elem = d_rec_elem; a.rec_vm = (const T *)d_rec_vm; a.seis = (T *)d_seis;
         a.d_it = d_it; a.step_off = 0;
+        a.persistent = (g.flags & SESNT_FLAG_PERSISTENT_ELEMENT) ? 1 : 0;
         return a;
     }
 };

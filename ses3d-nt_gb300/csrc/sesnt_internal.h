@@ -77,6 +77,7 @@ struct StepArgs {
     // step counter: it = *d_it + step_off
     const int *d_it;
     int step_off;
+    int persistent;  // element kernel: persistent prefetching variant (1) or one block per group (0)
 };
 
 // Kernel launchers for one polynomial degree and one precision, filled in by

@@ -26,6 +26,7 @@ OK = 0
 EINVAL, ECUDA, ENOMEM, ESTATE, ERANGE, ETIMEOUT, ENOTFOUND, EUNSUPPORTED, ENONFINITE = range(-1, -10, -1)
 FLAG_KAHAN = 1
 FLAG_NO_GRAPH = 2
+FLAG_PERSISTENT_ELEMENT = 4
 SOURCE_MT, SOURCE_SF = 0, 1
 WAVELETS = {"DELTA": 0, "RICKER": 1, "GAUSS": 2, "SIN**3": 3, "BRUNE": 4}
 CH_VX, CH_VY, CH_VZ = 1, 2, 4

@@ -257,6 +257,22 @@ def test_graph_and_chunked_runs_agree(gpu, sesnt_lib):
     assert rel_l2(b, a) < 1e-5 and rel_l2(c, a) < 1e-5
 
 
+@pytest.mark.parametrize("lpd,n_sls,aniso", [(4, 3, False), (4, 0, True), (6, 3, True), (7, 3, False), (2, 0, False)])
+def test_persistent_and_simple_element_kernels_agree(gpu, sesnt_lib, lpd, n_sls, aniso):
+    """The persistent prefetching element kernel and the one-block-per-group
+    kernel compute the same step (up to the order of the atomic adds)."""
+    wl = small_workload(lpd, n_sls=n_sls, aniso=aniso, nt=200)
+    a, fa, _ = run_gpu(wl, 200)
+    b, fb, _ = run_gpu(with_grid(wl, flags=sesnt.FLAG_PERSISTENT_ELEMENT), 200)
+    assert rel_l2(a, b) < 1e-5
+    for k in fa:
+        assert rel_l2(fa[k], fb[k]) < 1e-5, k
+    for prec in (8,):
+        c, _, _ = run_gpu(with_grid(wl, precision=prec), 200)
+        d, _, _ = run_gpu(with_grid(wl, precision=prec, flags=sesnt.FLAG_PERSISTENT_ELEMENT), 200)
+        assert rel_l2(c, d) < 1e-12
+
+
 def test_kahan_update(gpu, sesnt_lib, oracle_mod):
     wl = small_workload(4, nt=300)
     k, _, _ = run_gpu(with_grid(wl, flags=sesnt.FLAG_KAHAN), 300)

@@ -237,6 +237,74 @@ long long sesnt_footprint_bytes(const sesnt_grid_t *grid);
  * their own work after the library's. */
 void *sesnt_stream(const sesnt_t *h);
 
+/* ------------------------------------------------------------------------
+ * Files and configuration (host only, no GPU needed)
+ * ------------------------------------------------------------------------ */
+
+/* Message of the last failed call of this section on this thread. */
+const char *sesnt_io_last_error(void);
+const char *sesnt_config_last_error(void);
+
+/* Reads a raw model or field file: native float32 in the reference raw
+ * layout, no header, with the file-size check of src/mpi_parallel_io.F90:
+ * 300-309 (a size mismatch is SESNT_EINVAL, "wrong file size"). */
+int sesnt_read_raw_field(const char *path, int nx, int ny, int nz, int lpd, float *out);
+
+/* Writes a raw field (src/mpi_parallel_io.F90:121-190); an existing file is
+ * only replaced when override is nonzero. */
+int sesnt_write_raw_field(const char *path, int nx, int ny, int nz, int lpd, const float *data, int override);
+
+/* Header values of one SAC trace (src/sac_io/sac_io_mod.f90:178-222). Text
+ * fields need not be NUL-terminated; they are blank padded like Fortran
+ * CHARACTER assignments. date_time = [year, month, day, GMT offset minutes,
+ * hour, minute, second, millisecond] as in the &time group. */
+typedef struct sesnt_sac_info {
+    float lat, lon, depth, dt;
+    char network[8], station[8], location[8], channel[8], event[16];
+    int override;
+    int date_time[8];
+} sesnt_sac_info_t;
+
+/* Writes a SAC trace as the reference's receiver_cls%write does
+ * (src/config/receiver.f90:154-192, src/sac_io/sac_io_mod.f90:453-506). */
+int sesnt_write_sac(const char *path, const sesnt_sac_info_t *info, const float *data, int npts);
+
+/* "[network].[station].[location].[channel].sac" (auto_file_name,
+ * src/sac_io/sac_io_mod.f90:407-427). */
+int sesnt_sac_file_name(const sesnt_sac_info_t *info, char *out, int out_len);
+
+/* Day of the year of a Gregorian date (iday in src/sac_io/sac_header_mod.f90). */
+int sesnt_day_of_year(int year, int month, int day);
+
+/* Courant number (out[0]) and maximum resolved frequency in Hz (out[1]) of a
+ * model on a grid: cfl_loc and f_c_loc of src/model_paras.F90:464-561, in
+ * float32. Model arrays in the reference raw layout. */
+int sesnt_courant(const sesnt_grid_t *grid, const float *rhoinv, const float *lambda, const float *mu, float out[2]);
+
+/* The reference configuration file (NAMELIST groups, src/parser/parser.f90),
+ * parsed. */
+typedef struct sesnt_config sesnt_config_t;
+int sesnt_config_load(const char *path, sesnt_config_t **out);
+int sesnt_config_free(sesnt_config_t *cfg);
+/* Number of groups called `group` (e.g. "receiver"). */
+int sesnt_config_count(const sesnt_config_t *cfg, const char *group);
+/* &grid, &model and &time as a grid (precision 4, batch 1, n_sls 3 when a q
+ * model file is named). */
+int sesnt_config_grid(const sesnt_config_t *cfg, sesnt_grid_t *grid);
+/* Value of `key` in the idx-th `group` as text (several values separated by
+ * blanks; logicals as T/F). SESNT_ENOTFOUND when absent. */
+int sesnt_config_get(const sesnt_config_t *cfg, const char *group, int idx, const char *key, char *out, int out_len);
+/* JSON image of the whole file: {"group": [{key: value | [values]}...]}.
+ * With out == NULL only *needed (bytes incl. NUL) is set. */
+int sesnt_config_json(const sesnt_config_t *cfg, char *out, long long out_len, long long *needed);
+
+/* The reference forward workflow (src/ses3d-nt.F90:77-275, workflow
+ * 'forward') on the GPU: config, raw model files, sources (&source_mt,
+ * &source_sf with built-in wavelets), receivers (vx, vy, vz channels), all nt
+ * steps, one SAC file per receiver channel. precision 4 or 8. *n_traces gets
+ * the number of SAC files written. */
+int sesnt_forward(const char *config_path, int precision, int *n_traces);
+
 #ifdef __cplusplus
 }
 #endif

@@ -639,6 +639,56 @@ struct Sim {
         }
     }
 
+    // cfl_loc (src/model_paras.F90:529-561) and f_c_loc (:464-494) on the
+    // rank-6 fields, with cp/cs from init_auxiliary_model_parameters (:402-403).
+    void courant(T out[2]) const {
+        std::vector<T> cp(nloc), cs(nloc), th(nloc), ph(nloc);
+        for (int k = 0; k < P; ++k)
+            for (int j = 0; j < P; ++j)
+                for (int i = 0; i < P; ++i)
+                    for (int ez = 0; ez < nz; ++ez)
+                        for (int ey = 0; ey < ny; ++ey)
+                            for (int ex = 0; ex < nx; ++ex) {
+                                size_t a = I(E(ex, ey, ez), i, j, k);
+                                cp[a] = std::sqrt((lambda[a] + T(2) * mu[a]) * rhoinv[a]);
+                                cs[a] = std::sqrt(mu[a] * rhoinv[a]);
+                                th[a] = x1[(size_t)ex * P + i];
+                                ph[a] = y1[(size_t)ey * P + j];
+                            }
+        T cfl[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (size_t e = 0; e < nel; ++e)
+            for (int k = 0; k < P; ++k)
+                for (int j = 0; j < P; ++j)
+                    for (int i = 0; i < P; ++i) {
+                        size_t a = I(e, i, j, k);
+                        T vmax = (cs[a] < cp[a]) ? cp[a] : cs[a];  // MERGE(cp, cs, cs < cp)
+                        if (i >= 1) cfl[0] = std::max(cfl[0], vmax / (r[a] * (th[a] - th[I(e, i - 1, j, k)])));
+                        if (j >= 1) cfl[1] = std::max(cfl[1], vmax / (r_sin[a] * (ph[a] - ph[I(e, i, j - 1, k)])));
+                        if (k >= 1) cfl[2] = std::max(cfl[2], vmax / (r[I(e, i, j, k - 1)] - r[a]));
+                    }
+        T fc[3] = {INFINITY, INFINITY, INFINITY};
+        const T s = 2;
+        for (size_t e = 0; e < nel; ++e)
+            for (int b = 0; b < P; ++b)
+                for (int c = 0; c < P; ++c) {
+                    T sx = 0, sy = 0, sz = 0;
+                    for (int q = 0; q < P; ++q) {
+                        size_t ax = I(e, q, b, c), ay = I(e, b, q, c), az = I(e, b, c, q);
+                        sx = sx + ((cs[ax] > cp[ax]) ? cp[ax] : cs[ax]);
+                        sy = sy + ((cs[ay] > cp[ay]) ? cp[ay] : cs[ay]);
+                        sz = sz + ((cs[az] > cp[az]) ? cp[az] : cs[az]);
+                    }
+                    T vx = sx / T(P), vy = sy / T(P), vz = sz / T(P);
+                    T arcx = r[I(e, 0, b, c)] * ext.dx_elm;
+                    T arcy = r_sin[I(e, b, 0, c)] * ext.dy_elm;
+                    if (vx > 0) fc[0] = std::min(fc[0], vx / s / arcx);
+                    if (vy > 0) fc[1] = std::min(fc[1], vy / s / arcy);
+                    if (vz > 0) fc[2] = std::min(fc[2], vz / s / ext.dz_elm);
+                }
+        out[0] = std::max(cfl[0] * dt, std::max(cfl[1] * dt, cfl[2] * dt));
+        out[1] = std::min(fc[0], std::min(fc[1], fc[2]));
+    }
+
     // Forward loop: src/ses3d-nt.F90:240-270.
     void run(int nsteps) {
         for (int n = 0; n < nsteps; ++n) {
@@ -899,6 +949,19 @@ int oracle_get_seismograms(void *hv, void *out) {
     };
     if (h->precision == 8) return go(S<double>(h));
     return go(S<float>(h));
+}
+
+int oracle_courant(void *hv, float out[2]) {
+    Handle *h = (Handle *)hv;
+    if (h->precision == 8) {
+        double o[2];
+        S<double>(h)->courant(o);
+        out[0] = (float)o[0];
+        out[1] = (float)o[1];
+    } else {
+        S<float>(h)->courant(out);
+    }
+    return 0;
 }
 
 int oracle_is_visco(void *hv) {

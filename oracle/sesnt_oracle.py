@@ -69,6 +69,7 @@ def lib():
         _L.oracle_assemble_f32.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, fp]
         _L.oracle_stf.argtypes = [C.c_int, C.c_float, C.c_float, C.c_float, C.c_int, fp]
         _L.oracle_threads.argtypes = [C.c_int]
+        _L.oracle_courant.argtypes = [V, fp]
     return _L
 
 
@@ -192,6 +193,11 @@ class Oracle:
         out = np.zeros((self.nrec, 3, self.grid.nt), dt)
         lib().oracle_get_seismograms(self._h, out.ctypes.data_as(C.c_void_p))
         return out
+
+    def courant(self):
+        out = np.zeros(2, np.float32)
+        lib().oracle_courant(self._h, _fp(out))
+        return float(out[0]), float(out[1])
 
     def visco(self):
         return bool(lib().oracle_is_visco(self._h))

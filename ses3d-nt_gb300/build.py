@@ -16,6 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libsesnt.so")
+CLI = os.path.join(HERE, "ses3d-nt-gpu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -64,6 +65,10 @@ def build(verbose=False, extra_nvcc=()):
     objs = [o for _, o in jobs]
     _run([nvcc, *ARCH, "-shared", "-o", LIB + ".tmp", *objs, "-Xcompiler", "-fPIC"])
     os.replace(LIB + ".tmp", LIB)
+    # command-line driver linked against the library (found next to it)
+    _run(["g++", "-O2", "-std=c++17", "-o", CLI + ".tmp", os.path.join(HERE, "cli", "ses3d-nt-gpu.cpp"),
+          "-L" + HERE, "-lsesnt", "-Wl,-rpath,$ORIGIN"])
+    os.replace(CLI + ".tmp", CLI)
     return LIB
 
 

@@ -94,6 +94,13 @@ class Grid:
         return (self.nx * n + 1) * (self.ny * n + 1) * (self.nz * n + 1)
 
 
+class _SacInfo(C.Structure):
+    _fields_ = [("lat", C.c_float), ("lon", C.c_float), ("depth", C.c_float), ("dt", C.c_float),
+                ("network", C.c_char * 8), ("station", C.c_char * 8), ("location", C.c_char * 8),
+                ("channel", C.c_char * 8), ("event", C.c_char * 16), ("override", C.c_int),
+                ("date_time", C.c_int * 8)]
+
+
 _lib = None
 
 
@@ -139,6 +146,21 @@ def lib():
         "sesnt_info": (I, [P, C.POINTER(C.c_longlong)]),
         "sesnt_footprint_bytes": (C.c_longlong, [G]),
         "sesnt_stream": (P, [P]),
+        "sesnt_io_last_error": (C.c_char_p, []),
+        "sesnt_config_last_error": (C.c_char_p, []),
+        "sesnt_read_raw_field": (I, [C.c_char_p, I, I, I, I, fp]),
+        "sesnt_write_raw_field": (I, [C.c_char_p, I, I, I, I, fp, I]),
+        "sesnt_write_sac": (I, [C.c_char_p, C.POINTER(_SacInfo), fp, I]),
+        "sesnt_sac_file_name": (I, [C.POINTER(_SacInfo), C.c_char_p, I]),
+        "sesnt_day_of_year": (I, [I, I, I]),
+        "sesnt_courant": (I, [G, fp, fp, fp, fp]),
+        "sesnt_config_load": (I, [C.c_char_p, C.POINTER(C.c_void_p)]),
+        "sesnt_config_free": (I, [P]),
+        "sesnt_config_count": (I, [P, C.c_char_p]),
+        "sesnt_config_grid": (I, [P, G]),
+        "sesnt_config_get": (I, [P, C.c_char_p, I, C.c_char_p, C.c_char_p, I]),
+        "sesnt_config_json": (I, [P, C.c_char_p, C.c_longlong, C.POINTER(C.c_longlong)]),
+        "sesnt_forward": (I, [C.c_char_p, I, C.POINTER(C.c_int)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -301,3 +323,119 @@ class Simulation:
         self._c(lib().sesnt_info(self._h, out))
         keys = ("elements", "n_loc", "n_uni", "device_bytes", "algorithmic_bytes_per_step", "launches_per_step")
         return dict(zip(keys, list(out)))
+
+
+# ---------------------------------------------------------------------------
+# files and configuration
+# ---------------------------------------------------------------------------
+def _io_check(rc, which="io"):
+    if rc < 0:
+        m = lib().sesnt_io_last_error() if which == "io" else lib().sesnt_config_last_error()
+        raise SesntError(rc, m.decode() if m else "")
+    return rc
+
+
+def read_raw_field(path, grid):
+    """A raw model/field file in the reference layout, with the size check."""
+    out = np.zeros(grid.n_loc, np.float32)
+    _io_check(lib().sesnt_read_raw_field(os.fsencode(path), grid.nx, grid.ny, grid.nz, grid.lpd, _fptr(out)))
+    return out.reshape(grid.shape, order="F")
+
+
+def write_raw_field(path, grid, field, override=False):
+    f = _f32(field, grid.n_loc)
+    _io_check(lib().sesnt_write_raw_field(os.fsencode(path), grid.nx, grid.ny, grid.nz, grid.lpd, _fptr(f),
+                                          int(bool(override))))
+
+
+def sac_info(lat, lon, depth, dt, network="Ses3d-NT", station="", location="", channel="", event="ses3d-nt event",
+             override=False, date_time=(2000, 1, 1, 0, 0, 0, 0, 0)):
+    i = _SacInfo()
+    i.lat, i.lon, i.depth, i.dt = lat, lon, depth, dt
+    i.network, i.station, i.location = network.encode()[:8], station.encode()[:8], location.encode()[:8]
+    i.channel, i.event = channel.encode()[:8], event.encode()[:16]
+    i.override = int(bool(override))
+    for q in range(8):
+        i.date_time[q] = int(date_time[q])
+    return i
+
+
+def write_sac(path, info, data):
+    d = np.ascontiguousarray(data, np.float32)
+    _io_check(lib().sesnt_write_sac(os.fsencode(path), C.byref(info), _fptr(d), d.size))
+
+
+def sac_file_name(info):
+    buf = C.create_string_buffer(256)
+    _io_check(lib().sesnt_sac_file_name(C.byref(info), buf, 256))
+    return buf.value.decode()
+
+
+def day_of_year(y, m, d):
+    return lib().sesnt_day_of_year(y, m, d)
+
+
+def courant(grid, rhoinv, lam, mu):
+    """(Courant number, maximum resolved frequency in Hz) of a model."""
+    out = np.zeros(2, np.float32)
+    g = grid.c()
+    n = grid.n_loc
+    arrs = [_f32(x, n) for x in (rhoinv, lam, mu)]
+    _io_check(lib().sesnt_courant(C.byref(g), *[_fptr(a) for a in arrs], _fptr(out)))
+    return float(out[0]), float(out[1])
+
+
+class Config:
+    """A reference configuration file (NAMELIST groups)."""
+
+    def __init__(self, path):
+        self._c = C.c_void_p()
+        _io_check(lib().sesnt_config_load(os.fsencode(path), C.byref(self._c)), "config")
+
+    def close(self):
+        if self._c:
+            lib().sesnt_config_free(self._c)
+            self._c = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def count(self, group):
+        return lib().sesnt_config_count(self._c, group.encode())
+
+    def get(self, group, key, idx=0):
+        buf = C.create_string_buffer(1 << 16)
+        rc = lib().sesnt_config_get(self._c, group.encode(), idx, key.encode(), buf, 1 << 16)
+        if rc == ENOTFOUND:
+            return None
+        _io_check(rc, "config")
+        return buf.value.decode()
+
+    def json(self):
+        import json as _json
+        need = C.c_longlong()
+        _io_check(lib().sesnt_config_json(self._c, None, 0, C.byref(need)), "config")
+        buf = C.create_string_buffer(need.value)
+        _io_check(lib().sesnt_config_json(self._c, buf, need.value, None), "config")
+        return _json.loads(buf.value.decode())
+
+    def grid(self):
+        g = _Grid()
+        _io_check(lib().sesnt_config_grid(self._c, C.byref(g)), "config")
+        return Grid(nx=g.nx, ny=g.ny, nz=g.nz, lpd=g.lpd, lat_min=g.lat_min, lat_max=g.lat_max,
+                    lon_min=g.lon_min, lon_max=g.lon_max, rad_min=g.rad_min, rad_max=g.rad_max, dt=g.dt,
+                    nt=g.nt, taper_width=g.taper_width, taper_slope=g.taper_slope, n_sls=g.n_sls)
+
+
+def forward(config_path, precision=4):
+    """Run the reference forward workflow from a config file on the GPU;
+    returns the number of SAC traces written."""
+    n = C.c_int()
+    rc = lib().sesnt_forward(os.fsencode(config_path), precision, C.byref(n))
+    if rc < 0:
+        m = lib().sesnt_config_last_error()
+        raise SesntError(rc, m.decode() if m else "")
+    return n.value

@@ -160,8 +160,11 @@ def test_forward_from_config_file(gpu, sesnt_lib, oracle_mod, tmp_path, monkeypa
     ref = o.seismograms()
     names = {0: ("R01", "GB", "00", "vx vy vz"), 1: ("R02", "GB", "", "vx vz"), 2: ("R03", "Ses3d-NT", "", "vz")}
     for r, (sta, net, loc, chans) in names.items():
+        # relative to the receiver's whole record: on the central meridian
+        # some components vanish by symmetry and carry only rounding noise
+        scale = np.linalg.norm(ref[r])
+        assert scale > 0
         for ch in chans.split():
             data = np.fromfile("%s.%s.%s.%s.sac" % (net, sta, loc, ch), "<f4")[158:]
             c = "xyz".index(ch[1])
-            ref_c = ref[r, c]
-            assert np.linalg.norm(data - ref_c) / max(np.linalg.norm(ref_c), 1e-30) < 1e-4
+            assert np.linalg.norm(data - ref[r, c]) / scale < 1e-4, (sta, ch)

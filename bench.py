@@ -24,6 +24,7 @@ With torchrun (N>1) every rank runs an independent replica of the workload
 rank 0 prints the aggregate.
 """
 import argparse
+import copy
 import json
 import math
 import os
@@ -344,6 +345,75 @@ def e2e(args, wl):
             "seconds": el, "includes": "handle create, model upload, source/receiver set-up, K x (step + D2H samples)"}
 
 
+def run_served(args):
+    """Served stream: seeded requests (own grid, degree, step count, model
+    and 1..n sources) arriving as a Poisson process, served concurrently by
+    the request server, against the plain path (every source of every request
+    run alone, one after another). Sizes are the served workload's ranges
+    scaled down (see `ranges`) so that the run ends in minutes."""
+    import threading as _th
+
+    import numpy as np
+
+    import sesnt
+    import workloads
+    ranges = dict(lateral=(16, 48), radial=(8, 24), lpds=(4, 6), steps=(300, 1500), sources=(1, 8), receivers=16)
+    stream = workloads.served_stream(args.requests, seed=5, **ranges)
+    reqs = [workloads.request_of(w) for w in stream]
+    hbm, peak_kind = peaks()
+
+    def alg_bytes(w):
+        g = w.grid
+        per_step = g.n_loc * (48 + 48 * g.n_sls + 8 + 4) * g.batch + g.n_uni * (24 * g.batch + 4)
+        return per_step * g.nt
+
+    total_updates = sum(w.grid.n_loc * w.grid.nt * w.grid.batch for w in stream)
+    total_bytes = sum(alg_bytes(w) for w in stream)
+    # plain: one source at a time, one request after another
+    t0 = time.perf_counter()
+    for w in stream:
+        for s in w.sources:
+            g1 = copy.copy(w.grid)
+            g1.batch = 1
+            one = copy.copy(s)
+            one.sim = 0
+            with sesnt.Simulation(g1) as sim:
+                workloads.setup(sim, workloads.Workload(w.name, g1, w.model, [one], w.receivers))
+                sim.run(1, g1.nt)
+                sim.seismograms()
+    plain_s = time.perf_counter() - t0
+    out = {"requests": len(stream), "ranges": {k: (list(v) if isinstance(v, tuple) else v) for k, v in ranges.items()},
+           "total_updates": total_updates, "plain": {"seconds": plain_s, "value": total_updates / plain_s}}
+    rng = np.random.default_rng(17)
+    for rate in args.rates:
+        gaps = rng.exponential(1.0 / rate, size=len(reqs))
+        with sesnt.Server(max_active=args.max_active, chunk_steps=64, max_batch=0) as srv:
+            ids = []
+
+            def feed():
+                for r, gap in zip(reqs, gaps):
+                    time.sleep(gap)
+                    ids.append(srv.submit(r))
+
+            t0 = time.perf_counter()
+            th = _th.Thread(target=feed)
+            th.start()
+            th.join()
+            for rid in ids:
+                srv.wait(rid, 3600.0)
+            wall = time.perf_counter() - t0
+            st = srv.stats()
+        out["served_rate_%g" % rate] = {
+            "arrival_rate_per_s": rate, "seconds": wall, "value": total_updates / wall,
+            "vs_plain": plain_s / wall, "latency_p50_s": st["latency_p50"], "latency_p99_s": st["latency_p99"],
+            "queue_wait_p50_s": st["queue_wait_p50"], "completed": st["completed"],
+            "hbm_frac_of_measured": total_bytes / wall / 1e9 / hbm}
+    return {"metric": METRIC + " (served stream)", "value": max(v["value"] for k, v in out.items()
+                                                                 if k.startswith("served")),
+            "unit": METRIC, "n_gpus": 1, "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic seeded request stream", "peak_source": peak_kind, "served": out}
+
+
 def run_reference(args):
     """CPU implementation of the path on the host cores (the oracle's
     restatement of the Fortran reference), same workload and metric."""
@@ -371,7 +441,11 @@ def main():
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="config2", choices=["config1", "config2", "config3", "config4"])
+    ap.add_argument("--workload", default="config2",
+                    choices=["config1", "config2", "config3", "config4", "served"])
+    ap.add_argument("--requests", type=int, default=40, help="served stream: number of requests")
+    ap.add_argument("--rates", type=float, nargs="+", default=[2.0, 8.0], help="served stream: arrivals per second")
+    ap.add_argument("--max-active", type=int, default=16, help="served stream: concurrent batches")
     ap.add_argument("--profile-steps", type=int, default=20)
     ap.add_argument("--accuracy-steps", type=int, default=1500)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -382,7 +456,12 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
-    line = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if args.impl == "reference":
+        line = run_reference(args)
+    elif args.workload == "served":
+        line = run_served(args) if RANK == 0 else None
+    else:
+        line = run_ours(args)
     if RANK == 0 and line is not None:
         print(json.dumps(line), flush=True)
     if _pg is not None:

@@ -305,6 +305,65 @@ int sesnt_config_json(const sesnt_config_t *cfg, char *out, long long out_len, l
  * the number of SAC files written. */
 int sesnt_forward(const char *config_path, int precision, int *n_traces);
 
+/* ------------------------------------------------------------------------
+ * Serving many simulations on one GPU. No counterpart in the reference
+ * (which runs one event per MPI job); built on the entry points above.
+ * ------------------------------------------------------------------------ */
+
+typedef struct sesnt_server sesnt_server_t;
+
+typedef struct sesnt_server_config {
+    long long device_bytes; /* HBM budget for admitted work; <= 0: 85% of free memory */
+    int max_active;         /* simultaneously running simulation batches (<= 0: 16) */
+    int chunk_steps;        /* steps a batch advances per scheduling turn (<= 0: 64) */
+    int max_batch;          /* simulations per batch (<= 0: all sources of a request) */
+} sesnt_server_config_t;
+
+/* One forward request: a model, its sources (one simulation each) and a
+ * receiver set recorded in every simulation. Arrays are copied at submit. */
+typedef struct sesnt_request {
+    sesnt_grid_t grid;        /* grid.batch is ignored */
+    const float *rhoinv, *lambda, *mu, *a, *b, *c, *q; /* reference raw layout; a..q may be NULL */
+    int n_sources;
+    const int *src_elem;      /* [n_sources][3] element indices (0-based) */
+    const int *src_kind;      /* [n_sources] SESNT_SOURCE_* */
+    const float *src_vanderm; /* [n_sources][(lpd+1)^3] */
+    const float *src_comp;    /* [n_sources][6] (MT) or first 3 used (SF) */
+    const float *src_stf;     /* [n_sources][nt] */
+    int n_receivers;
+    const int *rec_elem;      /* [n_receivers][3] */
+    const float *rec_vanderm; /* [n_receivers][(lpd+1)^3] */
+    const unsigned *rec_mask; /* [n_receivers] SESNT_CH_* sets, or NULL for vx|vy|vz */
+} sesnt_request_t;
+
+typedef struct sesnt_server_stats {
+    long long completed, failed, queued, active;
+    long long device_bytes_used, device_bytes_budget;
+    long long total_updates;      /* GLL-point-updates of completed requests */
+    double latency_p50, latency_p99, latency_max, queue_wait_p50; /* seconds, submit to done */
+    double wall_seconds;          /* first submit to last completion (completed requests) */
+    double updates_per_second;    /* total_updates / wall_seconds */
+} sesnt_server_stats_t;
+
+/* Starts the scheduler thread on the current device. */
+int sesnt_server_create(const sesnt_server_config_t *cfg, sesnt_server_t **out);
+/* Stops the scheduler after the work in flight, frees everything. */
+int sesnt_server_destroy(sesnt_server_t *s);
+/* Queues a request; returns at once with its id. SESNT_ENOMEM if even one
+ * simulation of it can never fit the budget. */
+int sesnt_server_submit(sesnt_server_t *s, const sesnt_request_t *req, long long *id);
+/* Waits up to timeout_s seconds; SESNT_ETIMEOUT if not done by then. */
+int sesnt_server_wait(sesnt_server_t *s, long long id, double timeout_s);
+/* Seismograms [n_sources][n_receivers][3][nt] of a finished request and
+ * times[0] = latency (submit to done), times[1] = queue wait. */
+int sesnt_server_result(sesnt_server_t *s, long long id, float *seis, double times[2]);
+/* Forgets a finished request (frees its host copies and results). */
+int sesnt_server_release(sesnt_server_t *s, long long id);
+/* Cancels a request that has not started; started work is not interrupted. */
+int sesnt_server_cancel(sesnt_server_t *s, long long id);
+int sesnt_server_stats(sesnt_server_t *s, sesnt_server_stats_t *out);
+const char *sesnt_server_last_error(const sesnt_server_t *s);
+
 #ifdef __cplusplus
 }
 #endif

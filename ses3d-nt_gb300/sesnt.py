@@ -439,3 +439,140 @@ def forward(config_path, precision=4):
         m = lib().sesnt_config_last_error()
         raise SesntError(rc, m.decode() if m else "")
     return n.value
+
+
+# ---------------------------------------------------------------------------
+# request server
+# ---------------------------------------------------------------------------
+class _ServerConfig(C.Structure):
+    _fields_ = [("device_bytes", C.c_longlong), ("max_active", C.c_int), ("chunk_steps", C.c_int),
+                ("max_batch", C.c_int)]
+
+
+class _Request(C.Structure):
+    _fields_ = [("grid", _Grid)] + [(k, C.POINTER(C.c_float)) for k in
+                                    ("rhoinv", "lambda_", "mu", "a", "b", "c", "q")] + [
+        ("n_sources", C.c_int), ("src_elem", C.POINTER(C.c_int)), ("src_kind", C.POINTER(C.c_int)),
+        ("src_vanderm", C.POINTER(C.c_float)), ("src_comp", C.POINTER(C.c_float)),
+        ("src_stf", C.POINTER(C.c_float)), ("n_receivers", C.c_int), ("rec_elem", C.POINTER(C.c_int)),
+        ("rec_vanderm", C.POINTER(C.c_float)), ("rec_mask", C.POINTER(C.c_uint))]
+
+
+class _ServerStats(C.Structure):
+    _fields_ = [(k, C.c_longlong) for k in ("completed", "failed", "queued", "active", "device_bytes_used",
+                                            "device_bytes_budget", "total_updates")] + [
+        (k, C.c_double) for k in ("latency_p50", "latency_p99", "latency_max", "queue_wait_p50", "wall_seconds",
+                                  "updates_per_second")]
+
+
+def _server_lib():
+    L = lib()
+    if not getattr(L, "_server_ready", False):
+        P = C.c_void_p
+        for name, res, args in [
+                ("sesnt_server_create", C.c_int, [C.POINTER(_ServerConfig), C.POINTER(P)]),
+                ("sesnt_server_destroy", C.c_int, [P]),
+                ("sesnt_server_submit", C.c_int, [P, C.POINTER(_Request), C.POINTER(C.c_longlong)]),
+                ("sesnt_server_wait", C.c_int, [P, C.c_longlong, C.c_double]),
+                ("sesnt_server_result", C.c_int, [P, C.c_longlong, C.POINTER(C.c_float),
+                                                  C.POINTER(C.c_double)]),
+                ("sesnt_server_release", C.c_int, [P, C.c_longlong]),
+                ("sesnt_server_cancel", C.c_int, [P, C.c_longlong]),
+                ("sesnt_server_stats", C.c_int, [P, C.POINTER(_ServerStats)]),
+                ("sesnt_server_last_error", C.c_char_p, [P])]:
+            f = getattr(L, name)
+            f.restype, f.argtypes = res, args
+        L._server_ready = True
+    return L
+
+
+class Request:
+    """Host arrays of one request (model, located sources, receivers)."""
+
+    def __init__(self, grid, model, sources, receivers):
+        # sources: list of (elem(3), vanderm, kind, comp(6 or 3), stf(nt)); receivers: list of (elem, vanderm)
+        self.grid = grid
+        self.model = [None if model.get(k) is None else _f32(model[k], grid.n_loc)
+                      for k in ("rhoinv", "lambda", "mu", "a", "b", "c", "q")]
+        ns, nr = len(sources), len(receivers)
+        NP = (grid.lpd + 1) ** 3
+        self.src_elem = np.ascontiguousarray([s[0] for s in sources], np.int32).reshape(ns, 3)
+        self.src_vm = np.ascontiguousarray([s[1] for s in sources], np.float32).reshape(ns, NP)
+        self.src_kind = np.ascontiguousarray([s[2] for s in sources], np.int32)
+        comp = np.zeros((ns, 6), np.float32)
+        for i, s in enumerate(sources):
+            comp[i, :len(s[3])] = s[3]
+        self.src_comp = comp
+        self.src_stf = np.ascontiguousarray([s[4] for s in sources], np.float32).reshape(ns, grid.nt)
+        self.rec_elem = np.ascontiguousarray([r[0] for r in receivers], np.int32).reshape(nr, 3)
+        self.rec_vm = np.ascontiguousarray([r[1] for r in receivers], np.float32).reshape(nr, NP)
+
+    def c(self):
+        ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))
+        r = _Request()
+        r.grid = self.grid.c()
+        for name, arr in zip(("rhoinv", "lambda_", "mu", "a", "b", "c", "q"), self.model):
+            setattr(r, name, _fptr(arr) if arr is not None else C.POINTER(C.c_float)())
+        r.n_sources = len(self.src_kind)
+        r.src_elem, r.src_kind = ip(self.src_elem), ip(self.src_kind)
+        r.src_vanderm, r.src_comp, r.src_stf = _fptr(self.src_vm), _fptr(self.src_comp), _fptr(self.src_stf)
+        r.n_receivers = len(self.rec_elem)
+        r.rec_elem, r.rec_vanderm = ip(self.rec_elem), _fptr(self.rec_vm)
+        r.rec_mask = C.POINTER(C.c_uint)()
+        return r
+
+
+class Server:
+    """Queue of forward requests served concurrently on the current GPU."""
+
+    def __init__(self, device_bytes=0, max_active=16, chunk_steps=64, max_batch=0):
+        L = _server_lib()
+        self._s = C.c_void_p()
+        cfg = _ServerConfig(device_bytes, max_active, chunk_steps, max_batch)
+        _check(L.sesnt_server_create(C.byref(cfg), C.byref(self._s)))
+        self._req = {}
+
+    def submit(self, request):
+        rid = C.c_longlong()
+        cr = request.c()
+        rc = _server_lib().sesnt_server_submit(self._s, C.byref(cr), C.byref(rid))
+        if rc < 0:
+            raise SesntError(rc, (_server_lib().sesnt_server_last_error(self._s) or b"").decode())
+        self._req[rid.value] = request
+        return rid.value
+
+    def wait(self, rid, timeout=600.0):
+        return _server_lib().sesnt_server_wait(self._s, rid, timeout)
+
+    def result(self, rid):
+        r = self._req[rid]
+        g = r.grid
+        out = np.zeros((len(r.src_kind), len(r.rec_elem), 3, g.nt), np.float32)
+        times = (C.c_double * 2)()
+        rc = _server_lib().sesnt_server_result(self._s, rid, _fptr(out), times)
+        if rc < 0:
+            raise SesntError(rc, (_server_lib().sesnt_server_last_error(self._s) or b"").decode())
+        return out, times[0], times[1]
+
+    def release(self, rid):
+        self._req.pop(rid, None)
+        return _server_lib().sesnt_server_release(self._s, rid)
+
+    def cancel(self, rid):
+        return _server_lib().sesnt_server_cancel(self._s, rid)
+
+    def stats(self):
+        st = _ServerStats()
+        _check(_server_lib().sesnt_server_stats(self._s, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in _ServerStats._fields_}
+
+    def close(self):
+        if self._s:
+            _server_lib().sesnt_server_destroy(self._s)
+            self._s = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

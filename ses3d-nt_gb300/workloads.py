@@ -273,3 +273,53 @@ def setup(sim, wl):
     for r in wl.receivers:
         elem, vm = locate_point(g, r.lat, r.lon, r.depth)
         sim.add_receiver(elem, vm)
+
+
+def request_of(wl):
+    """A sesnt.Request (model, located sources with their STFs, receivers)
+    for a workload whose sources are numbered 0..n-1 by `sim`."""
+    import sesnt
+    g = wl.grid
+    srcs = []
+    for s in sorted(wl.sources, key=lambda x: x.sim):
+        elem, vm = sesnt.locate_point(g, s.lat, s.lon, s.depth)
+        stf = sesnt.source_signature(s.wavelet, s.onset, s.width, g.dt, g.nt)
+        srcs.append((elem, vm, s.kind, np.asarray(s.comp, np.float32), stf))
+    recs = [sesnt.locate_point(g, r.lat, r.lon, r.depth) for r in wl.receivers]
+    return sesnt.Request(g, wl.model, srcs, recs)
+
+
+def served_stream(n_requests, seed, lateral=(16, 96), radial=(8, 48), lpds=(4, 6), steps=(500, 8000),
+                  sources=(1, 32), receivers=16):
+    """Seeded request stream of the served workload: per request a horizontal
+    element count uniform in `lateral` per direction, radial in `radial`, lpd
+    from `lpds`, step count log-uniform in `steps`, a config-2-generator model
+    with its own seed and 1..n random moment-tensor sources. Returns a list of
+    Workload objects (grid.batch = number of sources)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for q in range(n_requests):
+        nx = int(rng.integers(lateral[0], lateral[1] + 1))
+        ny = int(rng.integers(lateral[0], lateral[1] + 1))
+        nz = int(rng.integers(radial[0], radial[1] + 1))
+        lpd = int(rng.choice(lpds))
+        nt = int(round(math.exp(rng.uniform(math.log(steps[0]), math.log(steps[1])))))
+        ns = int(rng.integers(sources[0], sources[1] + 1))
+        # dt for a Courant number ~0.25 at the smallest GLL spacing: element
+        # sizes at the bottom of the section (r = 5771 km, colatitude 40 deg
+        # for phi) times the smallest GLL interval of the degree
+        elem_km = min(600.0 / nz, 5771.0 * math.radians(20.0) / nx,
+                      5771.0 * math.sin(math.radians(40.0)) * math.radians(20.0) / ny)
+        frac = float(np.diff(gll_points_f64(lpd)).min() / 2.0)
+        dt = float(min(0.25, 0.25 * elem_km * 1e3 * frac / 9400.0))
+        g = Grid(nx=nx, ny=ny, nz=nz, lpd=lpd, lat_min=30.0, lat_max=50.0, lon_min=0.0, lon_max=20.0,
+                 rad_min=5771000.0, rad_max=6371000.0, dt=dt, nt=nt,
+                 taper_width=min(2, (min(nx, ny, nz) - 1) // 2), taper_slope=1.2, n_sls=3, batch=ns)
+        model = gradient_model(g, int(rng.integers(1 << 30)))
+        srcs = random_sources(g, ns, rng)
+        for s in srcs:  # pulse early enough to be recorded in short runs
+            s.width = float(min(s.width, 0.1 * nt * dt + 4 * dt))
+            s.onset = 1.5 * s.width
+        out.append(Workload("request%d_%dx%dx%d_lpd%d_%dsrc_%dsteps" % (q, nx, ny, nz, lpd, ns, nt), g, model, srcs,
+                            surface_array(g, 4, receivers // 4, margin=2.5)))
+    return out

@@ -153,6 +153,14 @@ def make_workload(name, nt_needed):
         wl = workloads.config3(nt=4000)
     elif name == "config4":
         wl = workloads.config4(nt=3000)
+    elif name == "config4_plain":  # the config-4 grid and model with one source
+        wl = workloads.config4(nt=3000, batch=1)
+    elif name == "config1_batch64":  # the config-1 grid and model with 64 random sources
+        import numpy as _np
+        wl = workloads.config1(nt=2000)
+        wl.grid.batch = 64
+        wl.sources = workloads.random_sources(wl.grid, 64, _np.random.Generator(_np.random.PCG64(1)))
+        wl.name = "config1_batched_64src_12x12x8_lpd4"
     else:
         raise SystemExit("unknown workload " + name)
     wl.grid.nt = max(wl.grid.nt, nt_needed)
@@ -292,29 +300,31 @@ def run_ours(args):
 
 
 def accuracy(args, wl):
-    """FP32 vs FP64 build of the same kernels: relative L2 of seismograms and
-    of the final vz over the first accuracy_steps steps."""
-    import copy
-
+    """FP32 (plain and Kahan-compensated velocity update) against the FP64
+    build of the same kernels: relative L2 of the seismograms of the first
+    simulation and of its final vz after accuracy_steps steps."""
     import numpy as np
 
     import sesnt
     import workloads
     n = min(args.accuracy_steps, wl.grid.nt)
-    out = {}
     res = {}
-    for prec in (4, 8):
+    for name, prec, flags in (("fp32", 4, 0), ("fp32_kahan", 4, sesnt.FLAG_KAHAN), ("fp64", 8, 0)):
         w = copy.copy(wl)
         w.grid = copy.copy(wl.grid)
         w.grid.precision = prec
+        w.grid.flags = flags
+        w.grid.batch = 1
+        w.sources = [s for s in wl.sources if s.sim == 0]
         with sesnt.Simulation(w.grid) as sim:
             workloads.setup(sim, w)
             sim.run(1, n)
-            res[prec] = (sim.seismograms()[0].astype(np.float64), sim.field("vz", precision=8))
+            res[name] = (sim.seismograms()[0].astype(np.float64), sim.field("vz", precision=8))
     rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
-    out["steps"] = n
-    out["seismogram_rel_l2"] = rel(res[4][0], res[8][0])
-    out["vz_rel_l2"] = rel(res[4][1], res[8][1])
+    out = {"steps": n}
+    for name in ("fp32", "fp32_kahan"):
+        out[name] = {"seismogram_rel_l2": rel(res[name][0], res["fp64"][0]),
+                     "vz_rel_l2": rel(res[name][1], res["fp64"][1])}
     return out
 
 
@@ -442,7 +452,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="config2",
-                    choices=["config1", "config2", "config3", "config4", "served"])
+                    choices=["config1", "config2", "config3", "config4", "config4_plain", "config1_batch64",
+                             "served"])
     ap.add_argument("--requests", type=int, default=40, help="served stream: number of requests")
     ap.add_argument("--rates", type=float, nargs="+", default=[2.0, 8.0], help="served stream: arrivals per second")
     ap.add_argument("--max-active", type=int, default=16, help="served stream: concurrent batches")

@@ -219,8 +219,8 @@ def run_ours(args):
     KP = args.profile_steps
     wl = make_workload(args.workload, W + K + KP + 1)
     g = wl.grid
-    if args.element == "persistent":
-        g.flags |= sesnt.FLAG_PERSISTENT_ELEMENT
+    g.flags |= {"persistent": sesnt.FLAG_PERSISTENT_ELEMENT, "tc_tf32x3": sesnt.FLAG_TC_TF32X3,
+                "tc_bf16x3": sesnt.FLAG_TC_BF16X3}.get(args.element, 0)
     S = g.batch
     hbm, peak_kind = peaks()
 
@@ -275,7 +275,8 @@ def run_ours(args):
         line["kernels_ms_per_step"] = {"element": prof[0] / KP, "sources": prof[1] / KP, "node": prof[2] / KP,
                                        "receivers": prof[3] / KP}
         traffic = None
-        tr_path = os.path.join(ROOT, "profiles", "k_element_%s.traffic.json" % wl.name)
+        tr_path = os.path.join(ROOT, "profiles", "%s_%s.traffic.json"
+                               % ("k_element_tc" if args.element.startswith("tc_") else "k_element", wl.name))
         if os.path.exists(tr_path):
             try:
                 with open(tr_path) as f:
@@ -284,7 +285,8 @@ def run_ours(args):
                     traffic = tr.get("dram_bytes_per_launch")
             except Exception:
                 traffic = None
-        line["roofline"] = {"bound": "hbm", "kernel": "k_element", "achieved": ach, "peak": hbm,
+        kname = "k_element_tc" if args.element.startswith("tc_") else "k_element"
+        line["roofline"] = {"bound": "hbm", "kernel": kname, "achieved": ach, "peak": hbm,
                             "peak_source": peak_kind, "unit": "GB/s", "frac": ach / hbm,
                             "traffic": traffic, "alg_bytes_per_launch": eb}
     if args.accuracy_steps > 0 and RANK == 0:
@@ -309,7 +311,9 @@ def accuracy(args, wl):
     import workloads
     n = min(args.accuracy_steps, wl.grid.nt)
     res = {}
-    for name, prec, flags in (("fp32", 4, 0), ("fp32_kahan", 4, sesnt.FLAG_KAHAN), ("fp64", 8, 0)):
+    for name, prec, flags in (("fp32", 4, 0), ("fp32_kahan", 4, sesnt.FLAG_KAHAN),
+                              ("fp32_tc_tf32x3", 4, sesnt.FLAG_TC_TF32X3),
+                              ("fp32_tc_bf16x3", 4, sesnt.FLAG_TC_BF16X3), ("fp64", 8, 0)):
         w = copy.copy(wl)
         w.grid = copy.copy(wl.grid)
         w.grid.precision = prec
@@ -322,7 +326,7 @@ def accuracy(args, wl):
             res[name] = (sim.seismograms()[0].astype(np.float64), sim.field("vz", precision=8))
     rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
     out = {"steps": n}
-    for name in ("fp32", "fp32_kahan"):
+    for name in ("fp32", "fp32_kahan", "fp32_tc_tf32x3", "fp32_tc_bf16x3"):
         out[name] = {"seismogram_rel_l2": rel(res[name][0], res["fp64"][0]),
                      "vz_rel_l2": rel(res[name][1], res["fp64"][1])}
     return out
@@ -462,8 +466,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-seconds", type=float, default=60.0)
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
-    ap.add_argument("--element", default="simple", choices=["persistent", "simple"],
-                    help="element kernel variant (both compute the full step)")
+    ap.add_argument("--element", default="simple", choices=["persistent", "simple", "tc_tf32x3", "tc_bf16x3"],
+                    help="element kernel variant (all compute the full step; tc_*: tcgen05 contractions)")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")

@@ -48,6 +48,9 @@ extern "C" {
 /* flags (sesnt_grid_t.flags) */
 #define SESNT_FLAG_KAHAN 1u      /* compensated velocity update */
 #define SESNT_FLAG_NO_GRAPH 2u   /* sesnt_run launches kernels directly, no CUDA graph */
+#define SESNT_FLAG_TC_TF32X3 8u   /* derivative and divergence contractions on the tensor cores
+                                     (tcgen05) in split TF32 (3 products), FP32 accumulation */
+#define SESNT_FLAG_TC_BF16X3 16u  /* the same in split BF16 (3 products); FP32 wavefields only */
 #define SESNT_FLAG_PERSISTENT_ELEMENT 4u /* persistent element kernel that prefetches the next
                                             element groups with cp.async (same results) */
 

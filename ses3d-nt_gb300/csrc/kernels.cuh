@@ -27,6 +27,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "sesnt_internal.h"
 
@@ -97,39 +98,49 @@ __device__ __forceinline__ T taper_value(T px, T py, T pz, T inv_alpha) {
     return exp(-(T(0.1) * (p2 * p2)));
 }
 
-// One element-local point of the step, from the velocity slab in shared
-// memory and the point's own stress, memory variables and material: velocity
-// gradient (line contractions), spherical completion, stress rate (elastic or
-// standard linear solids, optional A,B,C), integration, taper of the stored
-// stress, memory-variable update, and the metric-weighted stresses of the
-// weak divergence written to the flux slab `my`.
-template <int N, typename T, int NSLS, bool ANISO>
-__device__ __forceinline__ void point_step(const StepArgs<T> &a, const T *sD, const T *svx, const T *svy,
-                                           const T *svz, int p, int i, int j, int k, int ex, int ey, int ez,
-                                           T lam, T mu, T tau, T cA, T cB, T cC, const T (&sg)[6],
-                                           const T (&m)[6][NSLS > 0 ? NSLS : 1], T *sig, T *mem, size_t nloc,
-                                           T *my) {
-    constexpr int P = N + 1, NP = P * P * P;
+// Per-point pieces of the element kernels. From the point's velocity
+// gradient and its stress, memory variables and material: spherical
+// completion, stress rate (elastic or standard linear solids, optional
+// A,B,C), integration, taper of the stored stress, memory-variable update,
+// and the metric-weighted stresses of the weak divergence written to the flux
+// slab `my` (9 x NP).
+// Raw velocity gradient at point (i,j,k): the nine line contractions of the
+// velocity slab with the scaled derivative tables (src/evolution.f90:130-159).
+// e[d*3 + c] = d-direction derivative of component c (d, c in x, y, z).
+template <int N, typename T>
+__device__ __forceinline__ void strain_contract(const T *sD, const T *svx, const T *svy, const T *svz, int i, int j,
+                                                int k, T (&e)[9]) {
+    constexpr int P = N + 1;
     const T *Dx = sD, *Dy = sD + P * P, *Dz = sD + 2 * P * P;
-    const T vx = svx[p], vy = svy[p], vz = svz[p];
-    // velocity gradient: line contractions along the three GLL directions
-    T exx = 0, exy = 0, exz = 0, eyy = 0, eyx = 0, eyz = 0, ezz = 0, ezy = 0, ezx = 0;
+#pragma unroll
+    for (int c = 0; c < 9; ++c) e[c] = 0;
 #pragma unroll
     for (int q = 0; q < P; ++q) {
         const int px_ = q + P * (j + P * k);
         const int py_ = i + P * (q + P * k);
         const int pz_ = i + P * (j + P * q);
         const T dx = Dx[q * P + i], dy = Dy[q * P + j], dz = Dz[q * P + k];
-        exx += svx[px_] * dx;
-        exy += svy[px_] * dx;
-        exz += svz[px_] * dx;
-        eyy += svy[py_] * dy;
-        eyx += svx[py_] * dy;
-        eyz += svz[py_] * dy;
-        ezz += svz[pz_] * dz;
-        ezy += svy[pz_] * dz;
-        ezx += svx[pz_] * dz;
+        e[0] += svx[px_] * dx;
+        e[1] += svy[px_] * dx;
+        e[2] += svz[px_] * dx;
+        e[3] += svx[py_] * dy;
+        e[4] += svy[py_] * dy;
+        e[5] += svz[py_] * dy;
+        e[6] += svx[pz_] * dz;
+        e[7] += svy[pz_] * dz;
+        e[8] += svz[pz_] * dz;
     }
+}
+
+// The rest of one element-local point's step, from its raw velocity gradient
+// e[9] (layout of strain_contract) and velocity.
+template <int N, typename T, int NSLS, bool ANISO>
+__device__ __forceinline__ void point_update(const StepArgs<T> &a, const T (&e)[9], T vx, T vy, T vz, int p, int i,
+                                             int j, int k, int ex, int ey, int ez, T lam, T mu, T tau, T cA, T cB,
+                                             T cC, const T (&sg)[6], const T (&m)[6][NSLS > 0 ? NSLS : 1], T *sig,
+                                             T *mem, size_t nloc, T *my) {
+    constexpr int P = N + 1, NP = P * P * P;
+    T exx = e[0], exy = e[1], exz = e[2], eyx = e[3], eyy = e[4], eyz = e[5], ezx = e[6], ezy = e[7], ezz = e[8];
     // spherical completion (theta = x, phi = y, r = z); divisions by r and
     // r*sin(theta) are products with tabulated reciprocals
     const T rr = a.r[ez * P + k], ir = a.inv_r[ez * P + k];
@@ -228,6 +239,19 @@ __device__ __forceinline__ void point_step(const StepArgs<T> &a, const T *sD, co
     my[6 * NP + p] = sxz * gx;
     my[7 * NP + p] = syz * gy;
     my[8 * NP + p] = szz * gz;
+}
+
+// One element-local point of the step with CUDA-core contractions.
+template <int N, typename T, int NSLS, bool ANISO>
+__device__ __forceinline__ void point_step(const StepArgs<T> &a, const T *sD, const T *svx, const T *svy,
+                                           const T *svz, int p, int i, int j, int k, int ex, int ey, int ez,
+                                           T lam, T mu, T tau, T cA, T cB, T cC, const T (&sg)[6],
+                                           const T (&m)[6][NSLS > 0 ? NSLS : 1], T *sig, T *mem, size_t nloc,
+                                           T *my) {
+    T e[9];
+    strain_contract<N, T>(sD, svx, svy, svz, i, j, k, e);
+    point_update<N, T, NSLS, ANISO>(a, e, svx[p], svy[p], svz[p], p, i, j, k, ex, ey, ez, lam, mu, tau, cA, cB, cC,
+                                    sg, m, sig, mem, nloc, my);
 }
 
 // Weak divergence at point (i,j,k): transposed line contractions over the
@@ -802,16 +826,27 @@ int prepare_variant() {
 
 // Kernel attributes (large dynamic shared memory) and the persistent grid
 // size, once per handle, outside stream capture.
+}  // namespace sesnt
+
+#include "element_tc.cuh"
+
+namespace sesnt {
+
 template <int N, typename T>
 int prepare_element() {
     if (prepare_variant<N, T, 0, false>() || prepare_variant<N, T, 0, true>() ||
         prepare_variant<N, T, kNsls, false>() || prepare_variant<N, T, kNsls, true>())
         return -1;
+    if constexpr (std::is_same_v<T, float>)
+        if (prepare_element_tc<N, 1>() || prepare_element_tc<N, 2>()) return -1;
     return 0;
 }
 
+
 template <int N, typename T>
 int launch_element(const StepArgs<T> &a, bool sls, bool aniso, void *stream) {
+    if constexpr (std::is_same_v<T, float>)
+        if (a.contraction) return launch_element_tc<N>(a, sls, aniso, stream);
     if (sls) return aniso ? launch_element_v<N, T, kNsls, true>(a, stream) : launch_element_v<N, T, kNsls, false>(a, stream);
     return aniso ? launch_element_v<N, T, 0, true>(a, stream) : launch_element_v<N, T, 0, false>(a, stream);
 }

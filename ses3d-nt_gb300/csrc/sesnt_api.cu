@@ -145,7 +145,8 @@ struct sesnt_handle {
     void *lam = nullptr, *mu = nullptr, *A = nullptr, *B = nullptr, *C = nullptr, *tau = nullptr;
     void *sig = nullptr, *mem = nullptr, *v = nullptr, *vc = nullptr, *F = nullptr, *invM = nullptr;
     int *d_it = nullptr;
-    double dt = 0, c1 = 0, c2 = 0, c3 = 0, jac = 0, alpha = 0;
+    int *d_err = nullptr;  // set by a kernel whose bounded wait ran out
+    double dt = 0, c1 = 0, c2 = 0, c3 = 0, jac = 0, alpha = 0, two_over_d[3] = {0, 0, 0};
     // sources and receivers
     std::vector<HostSource> sources;
     bool src_dirty = true;
@@ -176,6 +177,16 @@ struct sesnt_handle {
     }
     int cuda_fail(cudaError_t e, const char *what) {
         return fail(SESNT_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+    }
+    // After a synchronisation: the error word written by a kernel whose
+    // bounded completion wait ran out (the tensor-core element kernel).
+    int wait_status() {
+        if (!(g.flags & (SESNT_FLAG_TC_TF32X3 | SESNT_FLAG_TC_BF16X3))) return SESNT_OK;
+        int word = 0;
+        cudaError_t e = cudaMemcpy(&word, d_err, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(e, "reading the error word");
+        if (word) return fail(SESNT_ETIMEOUT, "a tensor-core completion wait ran out; the results of this run are invalid");
+        return SESNT_OK;
     }
     int alloc(void **out, size_t bytes, const char *what) {
         void *p = nullptr;
@@ -238,6 +249,11 @@ struct sesnt_handle {
         a.nrec = nrec_dev; a.rec_elem = d_rec_elem; a.rec_vm = (const T *)d_rec_vm; a.seis = (T *)d_seis;
         a.d_it = d_it; a.step_off = 0;
         a.persistent = (g.flags & SESNT_FLAG_PERSISTENT_ELEMENT) ? 1 : 0;
+        a.contraction = (g.flags & SESNT_FLAG_TC_TF32X3) ? 1 : ((g.flags & SESNT_FLAG_TC_BF16X3) ? 2 : 0);
+        a.two_over_d[0] = (T)two_over_d[0];
+        a.two_over_d[1] = (T)two_over_d[1];
+        a.two_over_d[2] = (T)two_over_d[2];
+        a.err = d_err;
         return a;
     }
 };
@@ -281,6 +297,12 @@ int check_grid(const sesnt_grid_t *g, std::string &why) {
     if (g->taper_width > 0 && !(g->taper_slope > 0.0f)) return bad("taper_slope must be positive");
     if (g->n_sls != 0 && g->n_sls != kNsls) return bad("n_sls must be 0 or 3");
     if (g->precision != 4 && g->precision != 8) return bad("precision must be 4 (FP32) or 8 (FP64)");
+    if ((g->flags & (SESNT_FLAG_TC_TF32X3 | SESNT_FLAG_TC_BF16X3)) == (SESNT_FLAG_TC_TF32X3 | SESNT_FLAG_TC_BF16X3))
+        return bad("choose one tensor-core contraction mode");
+    if ((g->flags & (SESNT_FLAG_TC_TF32X3 | SESNT_FLAG_TC_BF16X3)) && g->precision != 4) {
+        why = "tensor-core contractions are built for FP32 wavefields only";
+        return SESNT_EUNSUPPORTED;
+    }
     if (g->batch < 1) return bad("batch must be >= 1");
     const long long P = g->lpd + 1;
     const long long nuni = (g->nx * (long long)g->lpd + 1) * (g->ny * (long long)g->lpd + 1) *
@@ -307,6 +329,9 @@ int setup_tables(sesnt_t *h) {
     h->c1 = (2.0 / dx) * h->jac;                // src/evolution.f90:337-339
     h->c2 = (2.0 / dy) * h->jac;
     h->c3 = -((2.0 / dz) * h->jac);
+    h->two_over_d[0] = 2.0 / dx;
+    h->two_over_d[1] = 2.0 / dy;
+    h->two_over_d[2] = 2.0 / dz;
     h->dt = (double)(T)g.dt;
     h->alpha = (double)(T)g.taper_slope;
     std::vector<double> dl = lagrange_derivative_matrix<double>(N);
@@ -692,6 +717,7 @@ int get_seis_impl(sesnt_t *h, float *out) {
     if (e == cudaSuccess)
         e = cudaMemcpy(host.data(), h->d_seis, host.size() * sizeof(T), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return h->cuda_fail(e, "reading seismograms");
+    if ((rc = h->wait_status())) return rc;
     for (int s = 0; s < h->S; ++s)
         for (size_t r = 0; r < nrec; ++r)
             for (int c = 0; c < 3; ++c) {
@@ -823,7 +849,8 @@ int sesnt_create(const sesnt_grid_t *grid, sesnt_t **out) {
         {&h->lam, nloc * E, "lambda"}, {&h->mu, nloc * E, "mu"},
         {&h->sig, 6 * nloc * E * S, "stress"},
         {&h->v, 3 * nuni * E * S, "velocity"}, {&h->F, 3 * nuni * E * S, "force"},
-        {&h->invM, nuni * E, "inverse mass"}, {(void **)&h->d_it, sizeof(int), "step counter"}};
+        {&h->invM, nuni * E, "inverse mass"}, {(void **)&h->d_it, sizeof(int), "step counter"},
+        {(void **)&h->d_err, sizeof(int), "error word"}};
     for (auto &a : allocs)
         if ((rc = h->alloc(a.p, a.n, a.w))) {
             g_create_error = h->err;
@@ -851,6 +878,10 @@ int sesnt_create(const sesnt_grid_t *grid, sesnt_t **out) {
     if ((rc = zero_state(h.get()))) {
         g_create_error = h->err;
         return rc;
+    }
+    if (cudaMemset(h->d_err, 0, sizeof(int)) != cudaSuccess) {
+        g_create_error = "zeroing the error word failed";
+        return SESNT_ECUDA;
     }
     *out = h.release();
     return SESNT_OK;
@@ -975,7 +1006,7 @@ int sesnt_run_timed(sesnt_t *h, int it0, int nsteps, float *ms) {
     if (rc) return rc;
     if (e != cudaSuccess) return h->cuda_fail(e, "timed run");
     cudaEventElapsedTime(ms, h->ev0, h->ev1);
-    return SESNT_OK;
+    return h->wait_status();
 }
 
 int sesnt_run_profiled(sesnt_t *h, int it0, int nsteps, float ms[4]) {
@@ -1020,7 +1051,7 @@ int sesnt_run_profiled(sesnt_t *h, int it0, int nsteps, float ms[4]) {
     }
     for (auto &e : ev) cudaEventDestroy(e);
     if (rc) return rc;
-    return err == cudaSuccess ? SESNT_OK : h->cuda_fail(err, "profiled run");
+    return err == cudaSuccess ? h->wait_status() : h->cuda_fail(err, "profiled run");
 }
 
 int sesnt_get_samples(sesnt_t *h, int it, float *out) {
@@ -1050,7 +1081,8 @@ int sesnt_get_samples(sesnt_t *h, int it, float *out) {
 int sesnt_synchronize(sesnt_t *h) {
     if (!h) return SESNT_EINVAL;
     cudaError_t e = cudaStreamSynchronize(h->stream);
-    return e == cudaSuccess ? SESNT_OK : h->cuda_fail(e, "synchronize");
+    if (e != cudaSuccess) return h->cuda_fail(e, "synchronize");
+    return h->wait_status();
 }
 
 int sesnt_reset(sesnt_t *h) {

@@ -27,6 +27,8 @@ EINVAL, ECUDA, ENOMEM, ESTATE, ERANGE, ETIMEOUT, ENOTFOUND, EUNSUPPORTED, ENONFI
 FLAG_KAHAN = 1
 FLAG_NO_GRAPH = 2
 FLAG_PERSISTENT_ELEMENT = 4
+FLAG_TC_TF32X3 = 8
+FLAG_TC_BF16X3 = 16
 SOURCE_MT, SOURCE_SF = 0, 1
 WAVELETS = {"DELTA": 0, "RICKER": 1, "GAUSS": 2, "SIN**3": 3, "BRUNE": 4}
 CH_VX, CH_VY, CH_VZ = 1, 2, 4

@@ -53,6 +53,12 @@ extern "C" {
 #define SESNT_FLAG_TC_BF16X3 16u  /* the same in split BF16 (3 products); FP32 wavefields only */
 #define SESNT_FLAG_PERSISTENT_ELEMENT 4u /* persistent element kernel that prefetches the next
                                             element groups with cp.async (same results) */
+#define SESNT_FLAG_STRAIN 32u     /* keep the displacement gradient (src/evolution.f90:179-187):
+                                     9 more element-local fields read and written each step;
+                                     enables SESNT_FIELD_EXX .. _EZZ */
+#define SESNT_FLAG_ROTATION 64u   /* compute the rotation strain of the whole volume every step;
+                                     enables SESNT_FIELD_ROT_* after any step (without it they
+                                     are available after the steps of a rotation snapshot) */
 
 /* source kinds (sesnt_add_source) */
 #define SESNT_SOURCE_MT 0 /* moment tensor: comp = Mxx Mxy Mxz Myy Myz Mzz */
@@ -65,10 +71,27 @@ extern "C" {
 #define SESNT_WAVELET_SIN3 3
 #define SESNT_WAVELET_BRUNE 4
 
-/* receiver channels (sesnt_add_receiver), src/config/channel_mod.f90:505-592 */
+/* receiver channels (sesnt_add_receiver), the receiver channel classes of
+ * src/config/channel_mod.f90 (construct_channel_container_receiver :270-342):
+ * vx vy vz (:505-592; 'e' = vy, 'z' = vz), n = -vx (:532-540), rot_vx rot_vy
+ * rot_vz (:620-812), the recorded source fields mxx .. mzz and fx fy fz
+ * (:859-1095). */
 #define SESNT_CH_VX 1u
 #define SESNT_CH_VY 2u
 #define SESNT_CH_VZ 4u
+#define SESNT_CH_N 8u
+#define SESNT_CH_ROT_VX 16u
+#define SESNT_CH_ROT_VY 32u
+#define SESNT_CH_ROT_VZ 64u
+#define SESNT_CH_MXX 128u
+#define SESNT_CH_MXY 256u
+#define SESNT_CH_MXZ 512u
+#define SESNT_CH_MYY 1024u
+#define SESNT_CH_MYZ 2048u
+#define SESNT_CH_MZZ 4096u
+#define SESNT_CH_FX 8192u
+#define SESNT_CH_FY 16384u
+#define SESNT_CH_FZ 32768u
 
 /* fields (sesnt_get_field) */
 #define SESNT_FIELD_VX 0
@@ -83,6 +106,22 @@ extern "C" {
 #define SESNT_FIELD_TAPER 9
 #define SESNT_FIELD_MASS 10     /* assembled mass matrix MM */
 #define SESNT_FIELD_MEMORY 13   /* + comp*3 + k: Mxx,Myy,Mzz,Mxy,Mxz,Myz x 3 mechanisms */
+/* volume-snapshot fields (get_field, src/volume_snapshot.f90:192-298) */
+#define SESNT_FIELD_PRESSURE 40 /* -(sxx + syy + szz)/3 */
+#define SESNT_FIELD_EXX 41      /* strain from the displacement gradient (SESNT_FLAG_STRAIN) */
+#define SESNT_FIELD_EXY 42
+#define SESNT_FIELD_EXZ 43
+#define SESNT_FIELD_EYY 44
+#define SESNT_FIELD_EYZ 45
+#define SESNT_FIELD_EZZ 46
+#define SESNT_FIELD_ROT_VX 47   /* rotation rate as the reference evaluates it after a step */
+#define SESNT_FIELD_ROT_VY 48
+#define SESNT_FIELD_ROT_VZ 49
+#define SESNT_FIELD_LAMBDA 50   /* model fields held on the device */
+#define SESNT_FIELD_MU 51
+#define SESNT_FIELD_A 52
+#define SESNT_FIELD_B 53
+#define SESNT_FIELD_C 54
 
 typedef struct sesnt_handle sesnt_t;
 
@@ -193,6 +232,35 @@ int sesnt_get_seismograms(sesnt_t *h, float *out);
  * host each step in the reference (src/config/receiver.f90:136-142).
  * Synchronous; for a Fortran driver that keeps its own traces. */
 int sesnt_get_samples(sesnt_t *h, int it, float *out);
+
+/* One receiver channel of simulation `sim` (SESNT_CH_*, a single bit that
+ * was requested for that receiver), float32 [nt]. Synchronous. No single
+ * counterpart in the reference: channel_cls%data of one receiver channel
+ * (src/config/channel_mod.f90:44-50). */
+int sesnt_get_trace(sesnt_t *h, int sim, int receiver, unsigned channel, float *out);
+
+/* Replaces output_raw_cls%mpi_write (src/output_raw.f90:117-168) with the
+ * step window of volume_snapshot_cls (src/volume_snapshot.f90:123-135): after every step it with ts_start <= it <= ts_end and
+ * (it - ts_start) % ts_increment == 0, field `which` of simulation `sim` is
+ * copied asynchronously to pinned host memory and written by a background
+ * thread to "<prefix><attribute>_<it>.vol" in the reference raw layout
+ * (float32, Fortran order). ts_end <= 0 means nt; prefix NULL or "" means
+ * "./"; attribute NULL means the field's name (sesnt_field_name). Existing
+ * files are replaced only with override != 0. Returns the snapshot index or
+ * an error (range checks of the reference constructor, :71-113). */
+int sesnt_add_snapshot(sesnt_t *h, int sim, int which, int ts_start, int ts_increment, int ts_end,
+                       const char *prefix, const char *attribute, int override);
+
+/* Waits until every snapshot file queued so far is written; returns the
+ * first write error since the last call (message in sesnt_last_error). */
+int sesnt_snapshots_wait(sesnt_t *h);
+
+/* Name of a field (the attribute of get_field in
+ * src/volume_snapshot.f90:192-298) or NULL, and the field of a name
+ * (case-insensitive; "cs"/"vs", "cp"/"vp" aliases have no device field) or
+ * -1. */
+const char *sesnt_field_name(int which);
+int sesnt_field_id(const char *name);
 
 /* Copies field `which` (SESNT_FIELD_*) of simulation `sim` to `out` in the
  * reference raw layout (element-local copies of shared nodes included), as

@@ -327,7 +327,13 @@ struct Sim {
     std::vector<T> L, txx, txy, txz, tyy, tyz, tzz;  // step temporaries (automatic arrays at :109-119)
     struct Channel { int comp; std::vector<T> data; };
     struct Source { int ex, ey, ez; std::vector<T> vm; std::vector<Channel> ch; };
-    struct Receiver { int ex, ey, ez; std::vector<T> vm; std::vector<T> data[3]; };
+    // displacement gradient (src/elastic_vars.F90, integrated at
+    // src/evolution.f90:179-187), kept when keep_du is set
+    bool keep_du = false;
+    std::vector<T> dxux, dyuy, dzuz, dxuy, dyux, dxuz, dzux, dyuz, dzuy;
+    // channel bit b (b = 0..15, as the receiver channel mask) -> data; vx, vy,
+    // vz always recorded in data[0..2]
+    struct Receiver { int ex, ey, ez; unsigned mask; std::vector<T> vm; std::vector<T> data[16]; };
     std::vector<Source> sources;
     std::vector<Receiver> receivers;
     int it = 0;
@@ -435,6 +441,8 @@ struct Sim {
         for (auto *v : {&vx, &vy, &vz, &sx, &sy, &sz, &sxx, &sxy, &sxz, &syy, &syz, &szz, &exx, &eyy, &ezz, &exy,
                         &eyx, &exz, &ezx, &ezy, &eyz, &L, &txx, &txy, &txz, &tyy, &tyz, &tzz})
             v->assign(nloc, T(0));
+        if (keep_du)
+            for (auto *v : {&dxux, &dyuy, &dzuz, &dxuy, &dyux, &dxuz, &dzux, &dyuz, &dzuy}) v->assign(nloc, T(0));
         for (auto &s : src) s.assign(nloc, T(0));
         if (visco)
             for (auto &m : M)
@@ -495,6 +503,17 @@ struct Sim {
                     eyz[a] = -vy[a] / rr + eyz[a] / rs;
                     exy[a] = exy[a] / rr;
                     eyx[a] = -(vy[a] * ct / rr) + eyx[a] / rs;
+                    if (keep_du) {  // :179-187
+                        dzuz[a] = dzuz[a] + dt * ezz[a];
+                        dyuy[a] = dyuy[a] + dt * eyy[a];
+                        dxux[a] = dxux[a] + dt * exx[a];
+                        dzux[a] = dzux[a] + dt * ezx[a];
+                        dxuz[a] = dxuz[a] + dt * exz[a];
+                        dzuy[a] = dzuy[a] + dt * ezy[a];
+                        dyuz[a] = dyuz[a] + dt * eyz[a];
+                        dxuy[a] = dxuy[a] + dt * exy[a];
+                        dyux[a] = dyux[a] + dt * eyx[a];
+                    }
                     exy[a] = (exy[a] + eyx[a]) / two;
                     exz[a] = (exz[a] + ezx[a]) / two;
                     eyz[a] = (eyz[a] + ezy[a]) / two;
@@ -626,7 +645,17 @@ struct Sim {
         }
     }
 
-    // record_vx/vy/vz: src/config/channel_mod.f90:505-592.
+    // Rotation rates as get_field / record_rot_v* evaluate them after a step
+    // (src/volume_snapshot.f90:238-246, src/config/channel_mod.f90:620-812).
+    T rot(int c, size_t a) const {
+        if (c == 0) return -vy[a] / r[a] + eyz[a] / r_sin[a] + ezy[a];
+        if (c == 1) return -ezx[a] + (vx[a] - exz[a]) / r[a];
+        return (exy[a] + vy[a] * cot_t[a] - eyx[a] / sin_t[a]) / r[a];
+    }
+
+    // record_vx/vy/vz (src/config/channel_mod.f90:505-592), record_n
+    // (:532-540), record_rot_v* (:620-712), record_m** / record_f*
+    // (:859-1095): SUM over the element of vanderm times the quantity.
     void record(int it_) {
         for (auto &rc : receivers) {
             size_t e = E(rc.ex, rc.ey, rc.ez);
@@ -635,6 +664,19 @@ struct Sim {
                 T s = 0;
                 for (int p = 0; p < NP; ++p) s = s + rc.vm[p] * (*v3[c])[e + nel * p];
                 rc.data[c][it_ - 1] = s;
+            }
+            for (int b = 3; b < 16; ++b) {
+                if (!((rc.mask >> b) & 1u)) continue;
+                T s = 0;
+                for (int p = 0; p < NP; ++p) {
+                    const size_t a = e + nel * p;
+                    T q;
+                    if (b == 3) q = T(-1) * rc.vm[p] * vx[a];
+                    else if (b <= 6) q = rc.vm[p] * rot(b - 4, a);
+                    else q = rc.vm[p] * src[b - 7][a];
+                    s = s + q;
+                }
+                rc.data[b][it_ - 1] = s;
             }
         }
     }
@@ -885,14 +927,43 @@ int oracle_add_source(void *hv, int ex, int ey, int ez, const float *vm, int kin
     return go(S<float>(h));
 }
 
-int oracle_add_receiver(void *hv, int ex, int ey, int ez, const float *vm) {
+// Receiver with a channel mask (bits as the GPU library's SESNT_CH_*: vx vy
+// vz n rot_vx rot_vy rot_vz mxx mxy mxz myy myz mzz fx fy fz).
+int oracle_add_receiver_mask(void *hv, int ex, int ey, int ez, const float *vm, unsigned mask) {
     Handle *h = (Handle *)hv;
     auto go = [&](auto *s) {
         typename std::remove_pointer_t<decltype(s)>::Receiver rc;
         rc.ex = ex; rc.ey = ey; rc.ez = ez;
+        rc.mask = mask | 7u;
         rc.vm.assign(vm, vm + s->NP);
         for (auto &d : rc.data) d.assign(s->nt, 0);
         s->receivers.push_back(std::move(rc));
+        return 0;
+    };
+    if (h->precision == 8) return go(S<double>(h));
+    return go(S<float>(h));
+}
+
+int oracle_add_receiver(void *hv, int ex, int ey, int ez, const float *vm) {
+    return oracle_add_receiver_mask(hv, ex, ey, ez, vm, 7u);
+}
+
+// Keep the displacement gradient (call before oracle_set_model).
+void oracle_keep_strain(void *hv) {
+    Handle *h = (Handle *)hv;
+    if (h->precision == 8) S<double>(h)->keep_du = true;
+    else S<float>(h)->keep_du = true;
+}
+
+// One receiver channel (bit b of the mask), [nt] in the working precision.
+int oracle_get_trace(void *hv, int receiver, int bit, void *out) {
+    Handle *h = (Handle *)hv;
+    auto go = [&](auto *s) {
+        using T = typename std::remove_pointer_t<decltype(s)>::real_t;
+        if (receiver < 0 || receiver >= (int)s->receivers.size() || bit < 0 || bit > 15) return -1;
+        const auto &rc = s->receivers[receiver];
+        if (!((rc.mask >> bit) & 1u)) return -1;
+        std::memcpy(out, rc.data[bit].data(), s->nt * sizeof(T));
         return 0;
     };
     if (h->precision == 8) return go(S<double>(h));
@@ -908,13 +979,38 @@ int oracle_run(void *hv, int nsteps) {
 
 // which: 0..2 vx,vy,vz; 3..8 sxx,sxy,sxz,syy,syz,szz; 9 taper; 10 MM
 // (assembled); 11 r; 12 sin_theta; 13..30 memory variables (comp*3+k);
-// 31..39 exx,eyy,ezz,exy,exz,eyz,eyx,ezx,ezy (last step's strain rates).
+// 31..39 exx,eyy,ezz,exy,exz,eyz,eyx,ezx,ezy (last step's strain rates);
+// get_field of src/volume_snapshot.f90:192-298: 40 pressure, 41..46 exx exy
+// exz eyy eyz ezz (displacement gradient), 47..49 rot_vx rot_vy rot_vz, 50..54
+// lambda mu a b c.
 int oracle_get_field(void *hv, int which, void *out) {
     Handle *h = (Handle *)hv;
     auto go = [&](auto *s) {
         using T = typename std::remove_pointer_t<decltype(s)>::real_t;
         const std::vector<T> *f = nullptr;
+        std::vector<T> tmp;
+        if (which >= 40 && which <= 49) {
+            if (which >= 41 && which <= 46 && !s->keep_du) return -1;
+            tmp.resize(s->nloc);
+            for (size_t a = 0; a < s->nloc; ++a) {
+                T x;
+                switch (which) {
+                    case 40: x = T(-1) * (s->sxx[a] + s->syy[a] + s->szz[a]) / T(3); break;
+                    case 41: x = s->dxux[a]; break;
+                    case 42: x = (s->dxuy[a] + s->dyux[a]) / T(2); break;
+                    case 43: x = (s->dxuz[a] + s->dzux[a]) / T(2); break;
+                    case 44: x = s->dyuy[a]; break;
+                    case 45: x = (s->dyuz[a] + s->dzuy[a]) / T(2); break;
+                    case 46: x = s->dzuz[a]; break;
+                    default: x = s->rot(which - 47, a);
+                }
+                tmp[a] = x;
+            }
+            f = &tmp;
+        }
         switch (which) {
+            case 50: f = &s->lambda; break; case 51: f = &s->mu; break;
+            case 52: f = &s->A; break; case 53: f = &s->B; break; case 54: f = &s->C; break;
             case 0: f = &s->vx; break; case 1: f = &s->vy; break; case 2: f = &s->vz; break;
             case 3: f = &s->sxx; break; case 4: f = &s->sxy; break; case 5: f = &s->sxz; break;
             case 6: f = &s->syy; break; case 7: f = &s->syz; break; case 8: f = &s->szz; break;

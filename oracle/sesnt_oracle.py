@@ -57,6 +57,9 @@ def lib():
         _L.oracle_locate_cfg.argtypes = [C.POINTER(_Cfg), C.c_float, C.c_float, C.c_float, ip, fp]
         _L.oracle_add_source.argtypes = [V, C.c_int, C.c_int, C.c_int, fp, C.c_int, fp, fp]
         _L.oracle_add_receiver.argtypes = [V, C.c_int, C.c_int, C.c_int, fp]
+        _L.oracle_add_receiver_mask.argtypes = [V, C.c_int, C.c_int, C.c_int, fp, C.c_uint]
+        _L.oracle_keep_strain.argtypes = [V]
+        _L.oracle_get_trace.argtypes = [V, C.c_int, C.c_int, V]
         _L.oracle_run.argtypes = [V, C.c_int]
         _L.oracle_get_field.argtypes = [V, C.c_int, V]
         _L.oracle_get_seismograms.argtypes = [V, V]
@@ -172,10 +175,24 @@ class Oracle:
         stf_ = np.ascontiguousarray(stf_, np.float32)
         lib().oracle_add_source(self._h, elem[0], elem[1], elem[2], _fp(vm), kind, _fp(comp), _fp(stf_))
 
-    def add_receiver(self, elem, vm):
+    def add_receiver(self, elem, vm, mask=7):
+        """mask: channel bits as the GPU library's SESNT_CH_* (vx vy vz always recorded)."""
         vm = np.ascontiguousarray(vm, np.float32)
-        lib().oracle_add_receiver(self._h, elem[0], elem[1], elem[2], _fp(vm))
+        lib().oracle_add_receiver_mask(self._h, elem[0], elem[1], elem[2], _fp(vm), mask)
         self.nrec += 1
+
+    def keep_strain(self):
+        """Integrate the displacement gradient (before set_model)."""
+        lib().oracle_keep_strain(self._h)
+
+    def trace(self, receiver, channel):
+        """One receiver channel (a single SESNT_CH_* bit), [nt]."""
+        bit = int(channel).bit_length() - 1
+        dt = np.float64 if self.precision == 8 else np.float32
+        out = np.zeros(self.grid.nt, dt)
+        if lib().oracle_get_trace(self._h, receiver, bit, out.ctypes.data_as(C.c_void_p)) != 0:
+            raise ValueError("channel %d of receiver %d unavailable" % (channel, receiver))
+        return out
 
     def run(self, nsteps):
         lib().oracle_run(self._h, nsteps)
@@ -203,9 +220,10 @@ class Oracle:
         return bool(lib().oracle_is_visco(self._h))
 
 
-def load_workload(o, wl, sim=0):
+def load_workload(o, wl, sim=0, masks=None):
     """Model, the sources of simulation `sim`, and all receivers of a workload,
-    located with the oracle's own point location."""
+    located with the oracle's own point location. masks: per-receiver channel
+    bits (default vx vy vz)."""
     m = wl.model
     o.set_model(m["rhoinv"], m["lambda"], m["mu"], m.get("a"), m.get("b"), m.get("c"), m.get("q"))
     kinds = {"DELTA": 0, "RICKER": 1, "GAUSS": 2, "SIN**3": 3, "BRUNE": 4}
@@ -216,6 +234,6 @@ def load_workload(o, wl, sim=0):
         elem, vm = locate(g, s.lat, s.lon, s.depth)
         o.add_source(elem, vm, s.kind, np.asarray(s.comp, np.float32),
                      stf(kinds[s.wavelet], s.onset, s.width, g.dt, g.nt))
-    for r in wl.receivers:
+    for q, r in enumerate(wl.receivers):
         elem, vm = locate(g, r.lat, r.lon, r.depth)
-        o.add_receiver(elem, vm)
+        o.add_receiver(elem, vm, 7 if masks is None else masks[q])

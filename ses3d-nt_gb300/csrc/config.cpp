@@ -11,6 +11,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <ctime>
+#include <limits>
 #include <map>
 #include <memory>
 #include <sstream>
@@ -467,6 +468,30 @@ int sesnt_forward(const char *config_path, int precision, int *n_traces) {
             return rc;
         }
     }
+    // &output_raw groups (src/output_raw.f90:175-253): one snapshot series per
+    // attribute, with the defaults of volume_snapshot_cls' constructor
+    // (src/volume_snapshot.f90:71-113)
+    struct Raw { std::string attr, prefix; int start, inc, end; bool override; };
+    std::vector<Raw> raws;
+    for (int q = 0;; ++q) {
+        const Group *og = nth(cfg, "output_raw", q);
+        if (!og) break;
+        double start = 1, inc = -1, end = -1;
+        get_num(og, "timestep_start", start);
+        get_num(og, "timestep_increment", inc);
+        get_num(og, "timestep_end", end);
+        const std::string prefix = get_str(og, "prefix", "./");
+        const bool over = get_bool(og, "override", false);
+        if (const std::vector<Value> *at = og->find("attributes"))
+            for (auto &a : *at) {
+                std::string l = lower(a.text);
+                while (!l.empty() && l.back() == ' ') l.pop_back();
+                if (l.empty()) continue;
+                raws.push_back({l, prefix, (int)start, (int)inc, end < 0 ? g.nt : (int)end, over});
+                const int id = sesnt_field_id(l.c_str());
+                if (id >= SESNT_FIELD_EXX && id <= SESNT_FIELD_EZZ) g.flags |= SESNT_FLAG_STRAIN;
+            }
+    }
     sesnt_t *h = nullptr;
     if ((rc = sesnt_create(&g, &h))) {
         g_cfg_error = sesnt_last_error(nullptr);
@@ -477,6 +502,46 @@ int sesnt_forward(const char *config_path, int precision, int *n_traces) {
     if ((rc = sesnt_set_model(h, ptr(0), ptr(1), ptr(2), ptr(3), ptr(4), ptr(5), ptr(6)))) {
         g_cfg_error = sesnt_last_error(h);
         return rc;
+    }
+    for (const Raw &r : raws) {
+        // wavefield and device-held fields: snapshots written behind the steps
+        const int id = sesnt_field_id(r.attr.c_str());
+        const bool host = r.attr == "rho" || r.attr == "vs" || r.attr == "cs" || r.attr == "vp" || r.attr == "cp" ||
+                          r.attr == "q";
+        if (id >= 0 && id != SESNT_FIELD_MASS && !host) {
+            if ((rc = sesnt_add_snapshot(h, 0, id, r.start, r.inc, r.end, r.prefix.c_str(), r.attr.c_str(),
+                                         r.override ? 1 : 0)) < 0) {
+                g_cfg_error = sesnt_last_error(h);
+                return rc;
+            }
+            continue;
+        }
+        if (!host) {
+            std::fprintf(stderr, "warning: snapshot attribute '%s' not available on the GPU path; skipped\n",
+                         r.attr.c_str());
+            continue;
+        }
+        if (r.start < 1 || r.inc < 1 || r.inc > g.nt || r.end < r.start) {
+            g_cfg_error = "timestep range of &output_raw out of range";
+            return SESNT_ERANGE;
+        }
+        // static model fields (get_field, src/volume_snapshot.f90:259-285):
+        // rho = 1/rhoinv where rhoinv > 0 (src/model_paras.F90:399-403)
+        std::vector<float> f(n);
+        for (long long i = 0; i < n; ++i) {
+            const float ri = arr[0][i], rho = ri > 0.0f ? 1.0f / ri : 0.0f;
+            if (r.attr == "rho") f[i] = rho;
+            else if (r.attr == "vs" || r.attr == "cs") f[i] = std::sqrt(arr[2][i] / rho);
+            else if (r.attr == "vp" || r.attr == "cp") f[i] = std::sqrt((arr[1][i] + 2.0f * arr[2][i]) / rho);
+            else f[i] = arr[6].empty() ? std::numeric_limits<float>::max() : arr[6][i];
+        }
+        for (int it = r.start; it <= std::min(r.end, g.nt); it += r.inc) {
+            const std::string path = r.prefix + r.attr + "_" + std::to_string(it) + ".vol";
+            if ((rc = sesnt_write_raw_field(path.c_str(), g.nx, g.ny, g.nz, g.lpd, f.data(), r.override ? 1 : 0))) {
+                g_cfg_error = sesnt_io_last_error();
+                return rc;
+            }
+        }
     }
     const Group *tm = cfg->first("time");
     std::vector<float> vm(P * P * P), stf(g.nt), comp;
@@ -515,21 +580,43 @@ int sesnt_forward(const char *config_path, int precision, int *n_traces) {
             }
         }
     }
-    struct Rec { const Group *grp; int index; unsigned mask; double lat, lon, depth; };
+    struct Rec {
+        const Group *grp;
+        int index;
+        std::vector<std::pair<std::string, unsigned>> chans;  // attribute, channel bit
+        double lat, lon, depth;
+    };
     std::vector<Rec> recs;
     for (int r = 0;; ++r) {
         const Group *rg = nth(cfg, "receiver", r);
         if (!rg) break;
         double lat = 0, lon = 0, depth = 0;
         get_num(rg, "lat", lat); get_num(rg, "lon", lon); get_num(rg, "depth", depth);
+        // receiver attributes (construct_channel_container_receiver,
+        // src/config/channel_mod.f90:270-342); unknown ones are dropped with
+        // a warning (src/config/receiver.f90:389-398)
+        static const std::pair<const char *, unsigned> kAttr[] = {
+            {"vx", SESNT_CH_VX}, {"n", SESNT_CH_N}, {"vy", SESNT_CH_VY}, {"e", SESNT_CH_VY}, {"vz", SESNT_CH_VZ},
+            {"z", SESNT_CH_VZ}, {"rot_vx", SESNT_CH_ROT_VX}, {"rot_vy", SESNT_CH_ROT_VY},
+            {"rot_vz", SESNT_CH_ROT_VZ}, {"mxx", SESNT_CH_MXX}, {"mxy", SESNT_CH_MXY}, {"myx", SESNT_CH_MXY},
+            {"mxz", SESNT_CH_MXZ}, {"mzx", SESNT_CH_MXZ}, {"myy", SESNT_CH_MYY}, {"myz", SESNT_CH_MYZ},
+            {"mzy", SESNT_CH_MYZ}, {"mzz", SESNT_CH_MZZ}, {"fx", SESNT_CH_FX}, {"fy", SESNT_CH_FY},
+            {"fz", SESNT_CH_FZ}};
         unsigned mask = 0;
+        std::vector<std::pair<std::string, unsigned>> chans;
         if (const std::vector<Value> *at = rg->find("attributes"))
             for (auto &a : *at) {
-                const std::string l = lower(a.text);
-                if (l == "vx") mask |= SESNT_CH_VX;
-                else if (l == "vy") mask |= SESNT_CH_VY;
-                else if (l == "vz") mask |= SESNT_CH_VZ;
-                else std::fprintf(stderr, "warning: receiver channel '%s' not built on the GPU path; skipped\n", a.text.c_str());
+                std::string l = lower(a.text);
+                while (!l.empty() && l.back() == ' ') l.pop_back();
+                unsigned bit = 0;
+                for (auto &k : kAttr)
+                    if (l == k.first) bit = k.second;
+                if (!bit) {
+                    std::fprintf(stderr, "warning: unknown receiver attribute '%s' dropped\n", a.text.c_str());
+                    continue;
+                }
+                mask |= bit;
+                chans.push_back({l, bit});
             }
         if (!mask) continue;
         if (sesnt_locate_point(&g, (float)lat, (float)lon, (float)depth, elem, vm.data())) {
@@ -542,17 +629,17 @@ int sesnt_forward(const char *config_path, int precision, int *n_traces) {
             g_cfg_error = sesnt_last_error(h);
             return idx;
         }
-        recs.push_back({rg, idx, mask, lat, lon, depth});
+        recs.push_back({rg, idx, chans, lat, lon, depth});
     }
     if ((rc = sesnt_run(h, 1, g.nt))) {
         g_cfg_error = sesnt_last_error(h);
         return rc;
     }
-    std::vector<float> seis(recs.size() * 3 * (size_t)g.nt);
-    if (!recs.empty() && (rc = sesnt_get_seismograms(h, seis.data()))) {
+    if ((rc = sesnt_snapshots_wait(h))) {
         g_cfg_error = sesnt_last_error(h);
         return rc;
     }
+    std::vector<float> trace(g.nt);
     // date_time from &time, else now (src/config/config.F90:218-225)
     int dtm[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
     std::vector<float> dv;
@@ -566,10 +653,12 @@ int sesnt_forward(const char *config_path, int precision, int *n_traces) {
     }
     const std::string event = get_str(cfg->first("general"), "event_name", "ses3d-nt event");
     int written = 0;
-    const char *chname[3] = {"vx", "vy", "vz"};
     for (const Rec &r : recs)
-        for (int c = 0; c < 3; ++c) {
-            if (!((r.mask >> c) & 1u)) continue;
+        for (const auto &ch : r.chans) {
+            if ((rc = sesnt_get_trace(h, 0, r.index, ch.second, trace.data()))) {
+                g_cfg_error = sesnt_last_error(h);
+                return rc;
+            }
             sesnt_sac_info_t info;
             std::memset(&info, 0, sizeof info);
             info.lat = (float)r.lat;
@@ -579,14 +668,14 @@ int sesnt_forward(const char *config_path, int precision, int *n_traces) {
             put_field(info.network, get_str(r.grp, "network", "Ses3d-NT"), 8);  // default: parser.f90:438
             put_field(info.station, get_str(r.grp, "station", ""), 8);
             put_field(info.location, get_str(r.grp, "location", ""), 8);
-            put_field(info.channel, chname[c], 8);
+            put_field(info.channel, ch.first, 8);
             put_field(info.event, event, 16);
             info.override = get_bool(r.grp, "override", false) ? 1 : 0;
             std::memcpy(info.date_time, dtm, sizeof dtm);
             char name[256];
             sesnt_sac_file_name(&info, name, sizeof name);
             const std::string path = get_str(r.grp, "prefix", "./") + name;
-            if ((rc = sesnt_write_sac(path.c_str(), &info, seis.data() + ((size_t)r.index * 3 + c) * g.nt, g.nt))) {
+            if ((rc = sesnt_write_sac(path.c_str(), &info, trace.data(), g.nt))) {
                 g_cfg_error = sesnt_io_last_error();
                 return rc;
             }

@@ -29,6 +29,7 @@
 #include <algorithm>
 #include <type_traits>
 
+#include "sesnt.h"
 #include "sesnt_internal.h"
 
 namespace sesnt {
@@ -132,20 +133,19 @@ __device__ __forceinline__ void strain_contract(const T *sD, const T *svx, const
     }
 }
 
-// The rest of one element-local point's step, from its raw velocity gradient
-// e[9] (layout of strain_contract) and velocity.
-template <int N, typename T, int NSLS, bool ANISO>
-__device__ __forceinline__ void point_update(const StepArgs<T> &a, const T (&e)[9], T vx, T vy, T vz, int p, int i,
-                                             int j, int k, int ex, int ey, int ez, T lam, T mu, T tau, T cA, T cB,
-                                             T cC, const T (&sg)[6], const T (&m)[6][NSLS > 0 ? NSLS : 1], T *sig,
-                                             T *mem, size_t nloc, T *my) {
-    constexpr int P = N + 1, NP = P * P * P;
+// Spherical completion of the raw velocity gradient e[9] (layout of
+// strain_contract) at point (i, ., k) of element (ex, ., ez)
+// (src/evolution.f90:165-173; theta = x, phi = y, r = z). Divisions by r and
+// r*sin(theta) are products with tabulated reciprocals. Output g[9] in the
+// order kDu* (xx yy zz xy yx xz zx yz zy), not yet symmetrised.
+template <int N, typename T>
+__device__ __forceinline__ void complete_gradient(const StepArgs<T> &a, const T (&e)[9], T vx, T vy, T vz, int i,
+                                                  int k, int ex, int ez, T (&g)[9]) {
+    constexpr int P = N + 1;
     T exx = e[0], exy = e[1], exz = e[2], eyx = e[3], eyy = e[4], eyz = e[5], ezx = e[6], ezy = e[7], ezz = e[8];
-    // spherical completion (theta = x, phi = y, r = z); divisions by r and
-    // r*sin(theta) are products with tabulated reciprocals
-    const T rr = a.r[ez * P + k], ir = a.inv_r[ez * P + k];
-    const T st = a.sin_t[ex * P + i], ct = a.cot_t[ex * P + i];
-    const T rs = rr * st, irs = ir * a.inv_sin[ex * P + i];
+    const T ir = a.inv_r[ez * P + k];
+    const T ct = a.cot_t[ex * P + i];
+    const T irs = ir * a.inv_sin[ex * P + i];
     ezz = -ezz;
     eyy = eyy * irs + (vz + vx * ct) * ir;
     exx = (vz + exx) * ir;
@@ -155,6 +155,32 @@ __device__ __forceinline__ void point_update(const StepArgs<T> &a, const T (&e)[
     eyz = -vy * ir + eyz * irs;
     exy = exy * ir;
     eyx = -(vy * ct) * ir + eyx * irs;
+    g[kDuXX] = exx; g[kDuYY] = eyy; g[kDuZZ] = ezz;
+    g[kDuXY] = exy; g[kDuYX] = eyx; g[kDuXZ] = exz;
+    g[kDuZX] = ezx; g[kDuYZ] = eyz; g[kDuZY] = ezy;
+}
+
+// The rest of one element-local point's step, from its raw velocity gradient
+// e[9] (layout of strain_contract) and velocity. du: this point's
+// displacement gradient (stride nloc) or null.
+template <int N, typename T, int NSLS, bool ANISO>
+__device__ __forceinline__ void point_update(const StepArgs<T> &a, const T (&e)[9], T vx, T vy, T vz, int p, int i,
+                                             int j, int k, int ex, int ey, int ez, T lam, T mu, T tau, T cA, T cB,
+                                             T cC, const T (&sg)[6], const T (&m)[6][NSLS > 0 ? NSLS : 1], T *sig,
+                                             T *mem, size_t nloc, T *my, T *du) {
+    constexpr int P = N + 1, NP = P * P * P;
+    T g[9];
+    complete_gradient<N, T>(a, e, vx, vy, vz, i, k, ex, ez, g);
+    T exx = g[kDuXX], eyy = g[kDuYY], ezz = g[kDuZZ], exy = g[kDuXY], eyx = g[kDuYX], exz = g[kDuXZ],
+      ezx = g[kDuZX], eyz = g[kDuYZ], ezy = g[kDuZY];
+    const T rr = a.r[ez * P + k];
+    const T rs = rr * a.sin_t[ex * P + i];
+    if (du) {
+        // displacement gradient du += dt * (completed velocity gradient)
+        // before the symmetrisation (src/evolution.f90:179-187)
+#pragma unroll
+        for (int c = 0; c < 9; ++c) du[c * nloc] = du[c * nloc] + a.dt * g[c];
+    }
     exy = (exy + eyx) * T(0.5);
     exz = (exz + ezx) * T(0.5);
     eyz = (eyz + ezy) * T(0.5);
@@ -247,11 +273,11 @@ __device__ __forceinline__ void point_step(const StepArgs<T> &a, const T *sD, co
                                            const T *svz, int p, int i, int j, int k, int ex, int ey, int ez,
                                            T lam, T mu, T tau, T cA, T cB, T cC, const T (&sg)[6],
                                            const T (&m)[6][NSLS > 0 ? NSLS : 1], T *sig, T *mem, size_t nloc,
-                                           T *my) {
+                                           T *my, T *du) {
     T e[9];
     strain_contract<N, T>(sD, svx, svy, svz, i, j, k, e);
     point_update<N, T, NSLS, ANISO>(a, e, svx[p], svy[p], svz[p], p, i, j, k, ex, ey, ez, lam, mu, tau, cA, cB, cC,
-                                    sg, m, sig, mem, nloc, my);
+                                    sg, m, sig, mem, nloc, my, du);
 }
 
 // Weak divergence at point (i,j,k): transposed line contractions over the
@@ -341,7 +367,8 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::M
     if (act) {
         const T *svx = sv + le * 3 * NP;
         point_step<N, T, NSLS, ANISO>(a, sD, svx, svx + NP, svx + 2 * NP, p, i, j, k, ex, ey, ez, lam, mu, tau, cA,
-                                      cB, cC, sg, m, sig, mem, nloc, sf + le * 9 * NP);
+                                      cB, cC, sg, m, sig, mem, nloc, sf + le * 9 * NP,
+                                      a.du ? a.du + (size_t)s * 9 * nloc + li : nullptr);
     }
     __syncthreads();
     if (act) {
@@ -505,7 +532,8 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT) k_element_pf(const StepArgs<T>
             const T *svx = svb + b * 3 * SLAB + le * NP;
             point_step<N, T, NSLS, ANISO>(a, sD, svx, svx + SLAB, svx + 2 * SLAB, p, i, j, k, ex, ey, ez, lam, mu,
                                           tau, cA, cB, cC, sg, m, a.sig + (size_t)s * 6 * nloc + li,
-                                          a.mem + (size_t)s * 6 * MS * nloc + li, nloc, sf + le * 9 * NP);
+                                          a.mem + (size_t)s * 6 * MS * nloc + li, nloc, sf + le * 9 * NP,
+                                          a.du ? a.du + (size_t)s * 9 * nloc + li : nullptr);
         }
         __syncthreads();  // fluxes complete; buffer b free for the group after next
         if (idx + 2 * stride < ngroups) prefetch(b, idx + 2 * stride);
@@ -647,6 +675,12 @@ __global__ void __launch_bounds__(256) k_node(const StepArgs<T> a) {
     }
 }
 
+}  // namespace sesnt
+
+#include "channels.cuh"
+
+namespace sesnt {
+
 template <int N, typename T>
 __global__ void __launch_bounds__(128) k_receivers(const StepArgs<T> a) {
     constexpr int P = N + 1, NP = P * P * P;
@@ -683,6 +717,7 @@ __global__ void __launch_bounds__(128) k_receivers(const StepArgs<T> a) {
         out[(size_t)a.nt] = acc[1];
         out[2 * (size_t)a.nt] = acc[2];
     }
+    if (a.rec_xmask) record_extra<N, T>(a, r, s, it, lane, ex, ey, ez, vm);
 }
 
 // Inverse assembled mass matrix in FP64 (src/model_paras.F90:410-415):
@@ -910,7 +945,8 @@ const LpdOps<T> *lpd_ops_n() {
     static const LpdOps<T> ops = {
         &launch_element<N, T>,        &launch_node<N, T>,        &launch_sources<N, T>,
         &launch_receivers<N, T>,      &launch_inv_mass<N, T>,    &launch_gather_local<N, T>,
-        &launch_scatter_unique<N, T>, &launch_taper_local<N, T>, &prepare_element<N, T>, ElemCfg<N>::NT,
+        &launch_scatter_unique<N, T>, &launch_taper_local<N, T>, &launch_rot_strain<N, T>,
+        &launch_derived<N, T>,        &prepare_element<N, T>,    ElemCfg<N>::NT,
         sizeof(T) * (4 * ElemCfg<N>::P * ElemCfg<N>::P + ElemCfg<N>::EPB * 12 * ElemCfg<N>::NP)};
     return &ops;
 }

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cctype>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -16,6 +17,7 @@
 
 #include "../../include/sesnt.h"
 #include "sesnt_internal.h"
+#include "snapshot_writer.h"
 
 using namespace sesnt;
 
@@ -159,6 +161,30 @@ struct sesnt_handle {
     int *d_rec_elem = nullptr;
     void *d_rec_vm = nullptr, *d_seis = nullptr;
     int nrec_dev = 0;
+    // receiver channels beyond vx, vy, vz: per receiver the device-computed
+    // channel bits, first trace slot and rotation-strain slot; per (sim,
+    // receiver) the source record of its element
+    std::vector<int> rec_xslot;
+    std::vector<SrcRec> src_recs;
+    unsigned *d_rec_xmask = nullptr;
+    int *d_rec_xslot = nullptr, *d_rec_rot = nullptr, *d_rec_src = nullptr, *d_rot_elems = nullptr;
+    void *d_xseis = nullptr, *d_rot_rec = nullptr;
+    int nxtr = 0, nrot = 0;
+    // optional state: displacement gradient [S][9][nloc] (SESNT_FLAG_STRAIN)
+    // and the rotation strain of the whole volume [S][6][nloc]
+    void *du = nullptr, *rot_full = nullptr;
+    int rot_full_it = -1;  // step whose rotation strain rot_full holds
+    int last_it = 0;       // last step enqueued
+    // volume snapshots
+    struct Snapshot {
+        int sim, which, start, inc, end;
+        std::string prefix, attribute;
+        bool override;
+    };
+    std::vector<Snapshot> snaps;
+    void *snap_stage = nullptr;
+    int device = 0;
+    std::unique_ptr<SnapshotWriter> writer;
     // graph
     cudaGraphExec_t graph = nullptr;
     int graph_steps = 0;
@@ -220,6 +246,7 @@ struct sesnt_handle {
     ~sesnt_handle() {
         drop_graph();
         if (stream) cudaStreamSynchronize(stream);
+        writer.reset();  // writes what is queued, then joins
         for (auto &b : bufs) cudaFree(b.p);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
@@ -254,6 +281,10 @@ struct sesnt_handle {
         a.two_over_d[1] = (T)two_over_d[1];
         a.two_over_d[2] = (T)two_over_d[2];
         a.err = d_err;
+        a.du = (T *)du;
+        a.rec_xmask = nxtr > 0 ? d_rec_xmask : nullptr;
+        a.rec_xslot = d_rec_xslot; a.rec_rot = d_rec_rot; a.rec_src = d_rec_src;
+        a.xseis = (T *)d_xseis; a.rot_rec = (const T *)d_rot_rec; a.nxtr = nxtr; a.nrot = nrot;
         return a;
     }
 };
@@ -394,12 +425,16 @@ int zero_state(sesnt_t *h) {
         {h->v, E * 3 * (size_t)h->nuni * h->S},
         {h->vc, h->kahan ? E * 3 * (size_t)h->nuni * h->S : 0},
         {h->F, E * 3 * (size_t)h->nuni * h->S},
-        {h->d_seis, E * (size_t)h->S * h->rec_elem.size() * 3 * h->g.nt}};
+        {h->d_seis, E * (size_t)h->S * h->rec_elem.size() * 3 * h->g.nt},
+        {h->d_xseis, E * (size_t)h->S * h->nxtr * h->g.nt},
+        {h->du, E * 9 * (size_t)h->nloc * h->S}};
     for (auto &z : zs)
         if (z.p && z.n) {
             cudaError_t e = cudaMemsetAsync(z.p, 0, z.n, h->stream);
             if (e != cudaSuccess) return h->cuda_fail(e, "zeroing state");
         }
+    h->rot_full_it = -1;
+    h->last_it = 0;
     return SESNT_OK;
 }
 
@@ -412,6 +447,7 @@ int upload_sources(sesnt_t *h) {
     h->d_src = h->d_src_vm = h->d_src_data = nullptr;
     h->nsrc_rec = 0;
     h->src_dirty = false;
+    h->src_recs.clear();
     if (h->sources.empty()) return SESNT_OK;
     std::vector<SrcRec> recs;
     std::vector<T> vm, data;
@@ -451,6 +487,7 @@ int upload_sources(sesnt_t *h) {
     if ((rc = h->alloc(&h->d_src, recs.size() * sizeof(SrcRec), "source records"))) return rc;
     if ((rc = h->alloc(&h->d_src_vm, vm.size() * sizeof(T), "source weights"))) return rc;
     if ((rc = h->alloc(&h->d_src_data, std::max<size_t>(1, data.size()) * sizeof(T), "source data"))) return rc;
+    h->src_recs = recs;
     cudaError_t e = cudaMemcpy(h->d_src, recs.data(), recs.size() * sizeof(SrcRec), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(h->d_src_vm, vm.data(), vm.size() * sizeof(T), cudaMemcpyHostToDevice);
     if (e == cudaSuccess && !data.empty())
@@ -458,6 +495,85 @@ int upload_sources(sesnt_t *h) {
     if (e != cudaSuccess) return h->cuda_fail(e, "uploading sources");
     h->nsrc_rec = (int)recs.size();
     return SESNT_OK;
+}
+
+// Device tables of the receiver channels beyond vx, vy, vz (rotation rates,
+// recorded source fields): trace slots in receiver order, so traces of
+// receivers registered earlier keep their slots and samples.
+constexpr unsigned kDeviceChannels = 0xFFF0u;
+
+template <typename T>
+int upload_receiver_channels(sesnt_t *h) {
+    const size_t nrec = h->rec_elem.size();
+    std::vector<unsigned> xm(nrec);
+    std::vector<int> slot(nrec), rot(nrec, -1), rot_elems;
+    int nx = 0;
+    for (size_t r = 0; r < nrec; ++r) {
+        xm[r] = h->rec_mask[r] & kDeviceChannels;
+        slot[r] = nx;
+        nx += __builtin_popcount(xm[r]);
+        if (xm[r] & (SESNT_CH_ROT_VX | SESNT_CH_ROT_VY | SESNT_CH_ROT_VZ)) {
+            rot[r] = (int)rot_elems.size();
+            rot_elems.push_back(h->rec_elem[r]);
+        }
+    }
+    const size_t nt = h->g.nt, S = h->S;
+    std::vector<T> old;
+    const int old_nx = h->nxtr;
+    if (h->d_xseis && old_nx > 0) {
+        old.resize(S * old_nx * nt);
+        cudaError_t e = cudaMemcpy(old.data(), h->d_xseis, old.size() * sizeof(T), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return h->cuda_fail(e, "reading receiver traces");
+    }
+    for (void *p : {(void *)h->d_rec_xmask, (void *)h->d_rec_xslot, (void *)h->d_rec_rot, (void *)h->d_rot_elems,
+                    h->d_xseis, h->d_rot_rec})
+        h->release(p);
+    h->d_rec_xmask = nullptr;
+    h->d_rec_xslot = h->d_rec_rot = h->d_rot_elems = nullptr;
+    h->d_xseis = h->d_rot_rec = nullptr;
+    h->nxtr = h->nrot = 0;
+    h->rec_xslot = slot;
+    if (nx == 0) return SESNT_OK;
+    int rc;
+    if ((rc = h->alloc((void **)&h->d_rec_xmask, nrec * sizeof(unsigned), "receiver channels")) ||
+        (rc = h->alloc((void **)&h->d_rec_xslot, nrec * sizeof(int), "receiver trace slots")) ||
+        (rc = h->alloc((void **)&h->d_rec_rot, nrec * sizeof(int), "receiver rotation slots")) ||
+        (rc = h->alloc((void **)&h->d_rot_elems, std::max<size_t>(1, rot_elems.size()) * sizeof(int),
+                       "rotation elements")) ||
+        (rc = h->alloc(&h->d_rot_rec, std::max<size_t>(1, S * 6 * rot_elems.size() * h->NP) * sizeof(T),
+                       "rotation strain")) ||
+        (rc = h->alloc(&h->d_xseis, S * nx * nt * sizeof(T), "receiver traces")))
+        return rc;
+    std::vector<T> xs(S * nx * nt, T(0));
+    for (size_t s = 0; s < S && old_nx > 0; ++s)
+        std::copy(old.begin() + s * old_nx * nt, old.begin() + (s + 1) * old_nx * nt, xs.begin() + s * nx * nt);
+    cudaError_t e = cudaMemcpy(h->d_rec_xmask, xm.data(), nrec * sizeof(unsigned), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_rec_xslot, slot.data(), nrec * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_rec_rot, rot.data(), nrec * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !rot_elems.empty())
+        e = cudaMemcpy(h->d_rot_elems, rot_elems.data(), rot_elems.size() * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->d_xseis, xs.data(), xs.size() * sizeof(T), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return h->cuda_fail(e, "uploading receiver channels");
+    h->nxtr = nx;
+    h->nrot = (int)rot_elems.size();
+    return SESNT_OK;
+}
+
+// Source record of each (simulation, receiver element), for the recorded
+// source-field channels.
+int upload_receiver_sources(sesnt_t *h) {
+    h->release(h->d_rec_src);
+    h->d_rec_src = nullptr;
+    if (h->nxtr == 0) return SESNT_OK;
+    const size_t nrec = h->rec_elem.size();
+    std::vector<int> rs((size_t)h->S * nrec, -1);
+    for (size_t q = 0; q < h->src_recs.size(); ++q)
+        for (size_t r = 0; r < nrec; ++r)
+            if (h->src_recs[q].elem == h->rec_elem[r]) rs[(size_t)h->src_recs[q].sim * nrec + r] = (int)q;
+    int rc;
+    if ((rc = h->alloc((void **)&h->d_rec_src, rs.size() * sizeof(int), "receiver sources"))) return rc;
+    cudaError_t e = cudaMemcpy(h->d_rec_src, rs.data(), rs.size() * sizeof(int), cudaMemcpyHostToDevice);
+    return e == cudaSuccess ? SESNT_OK : h->cuda_fail(e, "uploading receiver sources");
 }
 
 template <typename T>
@@ -494,13 +610,15 @@ int upload_receivers(sesnt_t *h) {
     if (e == cudaSuccess) e = cudaMemcpy(h->d_seis, seis.data(), seis.size() * sizeof(T), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return h->cuda_fail(e, "uploading receivers");
     h->nrec_dev = (int)nrec;
-    return SESNT_OK;
+    int rc2 = upload_receiver_channels<T>(h);
+    return rc2 ? rc2 : upload_receiver_sources(h);
 }
 
 template <typename T>
 int prepare_run(sesnt_t *h) {
     if (!h->model_set) return h->fail(SESNT_ESTATE, "sesnt_set_model must be called before stepping");
     int rc;
+    const bool changed = h->src_dirty || h->rec_dirty;
     if (h->src_dirty) {
         h->drop_graph();
         if ((rc = upload_sources<T>(h))) return rc;
@@ -509,17 +627,24 @@ int prepare_run(sesnt_t *h) {
         h->drop_graph();
         if ((rc = upload_receivers<T>(h))) return rc;
     }
+    if (changed && (rc = upload_receiver_sources(h))) return rc;
     return SESNT_OK;
 }
 
 // Enqueue steps [it, it+n) given that *d_it == it: element, sources, node,
 // receivers per step.
 template <typename T>
-int enqueue_steps(sesnt_t *h, int n) {
+int enqueue_steps(sesnt_t *h, int n, bool rot_full = false) {
     const LpdOps<T> *o = ops<T>(h);
     StepArgs<T> a = h->args<T>();
+    rot_full = rot_full || (h->g.flags & SESNT_FLAG_ROTATION);
     for (int q = 0; q < n; ++q) {
         a.step_off = q;
+        // rotation strain from the velocity before this step's update
+        if (h->nrot > 0 && o->rot_strain(a, h->d_rot_elems, h->nrot, (T *)h->d_rot_rec, h->stream))
+            return h->fail(SESNT_ECUDA, "rotation-strain kernel launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+        if (rot_full && o->rot_strain(a, nullptr, h->nel, (T *)h->rot_full, h->stream))
+            return h->fail(SESNT_ECUDA, "rotation-strain kernel launch failed: %s", cudaGetErrorString(cudaGetLastError()));
         if (o->element(a, h->sls, h->aniso, h->stream)) return h->fail(SESNT_ECUDA, "element kernel launch failed: %s", cudaGetErrorString(cudaGetLastError()));
         if (o->sources(a, h->stream)) return h->fail(SESNT_ECUDA, "source kernel launch failed: %s", cudaGetErrorString(cudaGetLastError()));
         if (o->node(a, h->kahan, h->stream)) return h->fail(SESNT_ECUDA, "node kernel launch failed: %s", cudaGetErrorString(cudaGetLastError()));
@@ -554,13 +679,10 @@ int build_graph(sesnt_t *h) {
     return SESNT_OK;
 }
 
+// Steps it0 .. it0+nsteps-1 (prepared): graph replays and direct launches.
 template <typename T>
-int run_impl(sesnt_t *h, int it0, int nsteps) {
-    if (nsteps <= 0) return SESNT_OK;
-    if (it0 < 1 || it0 + nsteps - 1 > h->g.nt)
-        return h->fail(SESNT_ERANGE, "steps %d..%d outside 1..nt=%d", it0, it0 + nsteps - 1, h->g.nt);
+int run_steps(sesnt_t *h, int it0, int nsteps) {
     int rc;
-    if ((rc = prepare_run<T>(h))) return rc;
     k_set_it<<<1, 1, 0, h->stream>>>(h->d_it, it0);
     int left = nsteps;
     if (h->use_graph && nsteps >= kGraphSteps) {
@@ -572,6 +694,132 @@ int run_impl(sesnt_t *h, int it0, int nsteps) {
         }
     }
     if (left > 0 && (rc = enqueue_steps<T>(h, left))) return rc;
+    h->last_it = it0 + nsteps - 1;
+    if (h->g.flags & SESNT_FLAG_ROTATION) h->rot_full_it = h->last_it;
+    return SESNT_OK;
+}
+
+// volume_snapshot_cls%process (src/volume_snapshot.f90:123-135)
+bool snapshot_due(const sesnt_handle::Snapshot &q, int it) {
+    return it >= q.start && it <= q.end && (it - q.start) % q.inc == 0;
+}
+
+// First step in [it, last] at which a snapshot is due, or last + 1.
+int next_snapshot_step(const sesnt_t *h, int it, int last) {
+    int best = last + 1;
+    for (const auto &q : h->snaps) {
+        int c = it <= q.start ? q.start : q.start + ((it - q.start + q.inc - 1) / q.inc) * q.inc;
+        if (c <= q.end && c < best) best = c;
+    }
+    return best;
+}
+
+bool is_rotation(int which) { return which >= SESNT_FIELD_ROT_VX && which <= SESNT_FIELD_ROT_VZ; }
+
+// Enqueues field `which` of simulation `sim` as an element-local array on the
+// handle's stream: either computed into `scratch` or a pointer into the state.
+// Sets *inverse when the host must invert the values (the mass matrix).
+template <typename T>
+int field_source(sesnt_t *h, int sim, int which, T *scratch, const T **out, bool *inverse) {
+    const LpdOps<T> *o = ops<T>(h);
+    StepArgs<T> a = h->args<T>();
+    const size_t nloc = (size_t)h->nloc, nuni = (size_t)h->nuni;
+    *out = scratch;
+    *inverse = false;
+    int rc = 0;
+    if (which >= 0 && which <= 2) {
+        rc = o->gather_local(a, (const T *)h->v + ((size_t)sim * 3 + which) * nuni, scratch, h->stream);
+    } else if (which >= 3 && which <= 8) {
+        *out = (const T *)h->sig + ((size_t)sim * 6 + (which - 3)) * nloc;
+    } else if (which == SESNT_FIELD_TAPER) {
+        rc = o->taper_local(a, scratch, h->stream);
+    } else if (which == SESNT_FIELD_MASS) {
+        rc = o->gather_local(a, (const T *)h->invM, scratch, h->stream);
+        *inverse = true;
+    } else if (which >= SESNT_FIELD_MEMORY && which < SESNT_FIELD_MEMORY + 6 * kNsls && h->sls) {
+        const int c = (which - SESNT_FIELD_MEMORY) / kNsls, q = (which - SESNT_FIELD_MEMORY) % kNsls;
+        *out = (const T *)h->mem + ((size_t)sim * 6 * kNsls + c * kNsls + q) * nloc;
+    } else if (which == SESNT_FIELD_PRESSURE) {
+        rc = o->derived(a, which, sim, nullptr, scratch, h->stream);
+    } else if (which >= SESNT_FIELD_EXX && which <= SESNT_FIELD_EZZ) {
+        if (!h->du) return h->fail(SESNT_ESTATE, "strain fields need SESNT_FLAG_STRAIN at sesnt_create");
+        rc = o->derived(a, which, sim, nullptr, scratch, h->stream);
+    } else if (is_rotation(which)) {
+        if (!h->rot_full || h->rot_full_it != h->last_it || h->last_it < 1)
+            return h->fail(SESNT_ESTATE, "rotation fields need SESNT_FLAG_ROTATION, or a rotation snapshot due at "
+                                         "the last step");
+        rc = o->derived(a, which, sim, (const T *)h->rot_full, scratch, h->stream);
+    } else if (which == SESNT_FIELD_LAMBDA) {
+        *out = (const T *)h->lam;
+    } else if (which == SESNT_FIELD_MU) {
+        *out = (const T *)h->mu;
+    } else if (which >= SESNT_FIELD_A && which <= SESNT_FIELD_C) {
+        void *src = which == SESNT_FIELD_A ? h->A : (which == SESNT_FIELD_B ? h->B : h->C);
+        if (src) {
+            *out = (const T *)src;
+        } else {
+            cudaError_t e = cudaMemsetAsync(scratch, 0, nloc * sizeof(T), h->stream);
+            if (e != cudaSuccess) return h->cuda_fail(e, "zeroing field");
+        }
+    } else {
+        return h->fail(SESNT_EINVAL, "unknown or unavailable field %d", which);
+    }
+    if (rc) return h->fail(SESNT_ECUDA, "field kernel failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return SESNT_OK;
+}
+
+// After step `it`: copy every snapshot due at `it` into a pinned buffer
+// behind the step's kernels and queue it for the writer thread.
+template <typename T>
+int capture_snapshots(sesnt_t *h, int it) {
+    for (const auto &q : h->snaps) {
+        if (!snapshot_due(q, it)) continue;
+        const T *src = nullptr;
+        bool inverse = false;
+        int rc = field_source<T>(h, q.sim, q.which, (T *)h->snap_stage, &src, &inverse);
+        if (rc) return rc;
+        void *buf = h->writer->acquire();
+        cudaError_t e = cudaMemcpyAsync(buf, src, (size_t)h->nloc * sizeof(T), cudaMemcpyDeviceToHost, h->stream);
+        cudaEvent_t ev = nullptr;
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(ev, h->stream);
+        if (e != cudaSuccess) {
+            if (ev) cudaEventDestroy(ev);
+            return h->cuda_fail(e, "snapshot copy");
+        }
+        const std::string path = q.prefix + q.attribute + "_" + std::to_string(it) + ".vol";
+        h->writer->submit(buf, ev, h->g.nx, h->g.ny, h->g.nz, h->g.lpd, (int)sizeof(T), path, q.override);
+    }
+    return SESNT_OK;
+}
+
+// The reference forward loop over steps it0 .. it0+nsteps-1: runs of steps
+// without snapshots go through run_steps; a step with snapshots due runs on
+// its own (with the whole-volume rotation strain when a rotation snapshot is
+// due) and is followed by the snapshot copies.
+template <typename T>
+int run_impl(sesnt_t *h, int it0, int nsteps) {
+    if (nsteps <= 0) return SESNT_OK;
+    if (it0 < 1 || it0 + nsteps - 1 > h->g.nt)
+        return h->fail(SESNT_ERANGE, "steps %d..%d outside 1..nt=%d", it0, it0 + nsteps - 1, h->g.nt);
+    int rc;
+    if ((rc = prepare_run<T>(h))) return rc;
+    if (h->snaps.empty()) return run_steps<T>(h, it0, nsteps);
+    const int last = it0 + nsteps - 1;
+    int it = it0;
+    while (it <= last) {
+        const int due = next_snapshot_step(h, it, last);
+        if (due > it && (rc = run_steps<T>(h, it, due - it))) return rc;
+        if (due > last) break;
+        bool rot = false;
+        for (const auto &q : h->snaps) rot = rot || (is_rotation(q.which) && snapshot_due(q, due));
+        k_set_it<<<1, 1, 0, h->stream>>>(h->d_it, due);
+        if ((rc = enqueue_steps<T>(h, 1, rot))) return rc;
+        h->last_it = due;
+        if (rot || (h->g.flags & SESNT_FLAG_ROTATION)) h->rot_full_it = due;
+        if ((rc = capture_snapshots<T>(h, due))) return rc;
+        it = due + 1;
+    }
     return SESNT_OK;
 }
 
@@ -588,39 +836,19 @@ void export_layout(const TI *in, TO *out, long long nel, int NP) {
 
 template <typename T>
 int get_field_impl(sesnt_t *h, int sim, int which, void *out, int out_prec) {
-    const LpdOps<T> *o = ops<T>(h);
-    StepArgs<T> a = h->args<T>();
-    const size_t nloc = (size_t)h->nloc, nuni = (size_t)h->nuni;
+    const size_t nloc = (size_t)h->nloc;
     void *scratch = nullptr;
     int rc;
     if ((rc = h->alloc(&scratch, nloc * sizeof(T), "field scratch"))) return rc;
-    T *loc = (T *)scratch;
     const T *src = nullptr;
     bool inverse = false;
-    if (which >= 0 && which <= 2) {
-        rc = o->gather_local(a, (const T *)h->v + ((size_t)sim * 3 + which) * nuni, loc, h->stream);
-    } else if (which >= 3 && which <= 8) {
-        src = (const T *)h->sig + ((size_t)sim * 6 + (which - 3)) * nloc;
-    } else if (which == SESNT_FIELD_TAPER) {
-        rc = o->taper_local(a, loc, h->stream);
-    } else if (which == SESNT_FIELD_MASS) {
-        rc = o->gather_local(a, (const T *)h->invM, loc, h->stream);
-        inverse = true;
-    } else if (which >= SESNT_FIELD_MEMORY && which < SESNT_FIELD_MEMORY + 6 * kNsls && h->sls) {
-        const int c = (which - SESNT_FIELD_MEMORY) / kNsls, q = (which - SESNT_FIELD_MEMORY) % kNsls;
-        src = (const T *)h->mem + ((size_t)sim * 6 * kNsls + c * kNsls + q) * nloc;
-    } else {
+    if ((rc = field_source<T>(h, sim, which, (T *)scratch, &src, &inverse))) {
         h->release(scratch);
-        return h->fail(SESNT_EINVAL, "unknown or unavailable field %d", which);
-    }
-    if (rc) {
-        h->release(scratch);
-        return h->fail(SESNT_ECUDA, "field kernel failed");
+        return rc;
     }
     std::vector<T> host(nloc);
     cudaError_t e = cudaStreamSynchronize(h->stream);
-    if (e == cudaSuccess)
-        e = cudaMemcpy(host.data(), src ? src : loc, nloc * sizeof(T), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(host.data(), src, nloc * sizeof(T), cudaMemcpyDeviceToHost);
     h->release(scratch);
     if (e != cudaSuccess) return h->cuda_fail(e, "reading field");
     if (inverse)
@@ -790,6 +1018,7 @@ size_t footprint(const sesnt_grid_t *g, bool aniso) {
     b += nloc * E * (2 + (aniso ? 3 : 0) + (g->n_sls ? 1 : 0));    // lambda, mu, A,B,C, tau
     b += nloc * E * S * (6 + (g->n_sls ? 6 * kNsls : 0));          // sigma, memory
     b += nuni * E * (1 + S * (6 + ((g->flags & SESNT_FLAG_KAHAN) ? 3 : 0)));  // invM, v, F, comp
+    b += nloc * E * S * (((g->flags & SESNT_FLAG_STRAIN) ? 9 : 0) + ((g->flags & SESNT_FLAG_ROTATION) ? 6 : 0));
     b += nloc * (sizeof(float) + E);                                // set_model staging + rhoinv (transient)
     b += 1 << 20;                                                   // tables, counters
     return b;
@@ -866,6 +1095,15 @@ int sesnt_create(const sesnt_grid_t *grid, sesnt_t **out) {
         g_create_error = h->err;
         return rc;
     }
+    if ((grid->flags & SESNT_FLAG_STRAIN) && (rc = h->alloc(&h->du, 9 * nloc * E * S, "displacement gradient"))) {
+        g_create_error = h->err;
+        return rc;
+    }
+    if ((grid->flags & SESNT_FLAG_ROTATION) && (rc = h->alloc(&h->rot_full, 6 * nloc * E * S, "rotation strain"))) {
+        g_create_error = h->err;
+        return rc;
+    }
+    cudaGetDevice(&h->device);
     if ((h->dbl ? lpd_ops<double>(h->N)->prepare() : lpd_ops<float>(h->N)->prepare()) != 0) {
         g_create_error = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(cudaGetLastError());
         return SESNT_ECUDA;
@@ -967,11 +1205,12 @@ int sesnt_add_source(sesnt_t *h, int sim, int ex, int ey, int ez, const float *v
 int sesnt_add_receiver(sesnt_t *h, int ex, int ey, int ez, const float *vanderm, unsigned channel_mask) {
     if (!h) return SESNT_EINVAL;
     if (!vanderm) return h->fail(SESNT_EINVAL, "vanderm is required");
+    if (channel_mask & ~0xFFFFu) return h->fail(SESNT_EINVAL, "unknown channel bits 0x%x", channel_mask & ~0xFFFFu);
     if (ex < 0 || ex >= h->g.nx || ey < 0 || ey >= h->g.ny || ez < 0 || ez >= h->g.nz)
         return h->fail(SESNT_ERANGE, "element (%d,%d,%d) outside the grid", ex, ey, ez);
     h->rec_elem.push_back(ex + h->g.nx * (ey + h->g.ny * ez));
     h->rec_vm.insert(h->rec_vm.end(), vanderm, vanderm + h->NP);
-    h->rec_mask.push_back(channel_mask & 7u);
+    h->rec_mask.push_back(channel_mask);
     h->rec_dirty = true;
     return (int)h->rec_elem.size() - 1;
 }
@@ -1027,6 +1266,9 @@ int sesnt_run_profiled(sesnt_t *h, int it0, int nsteps, float ms[4]) {
             StepArgs<T> a = h->args<T>();
             a.step_off = n;
             cudaEventRecord(ev[0], h->stream);
+            if (h->nrot > 0 && o->rot_strain(a, h->d_rot_elems, h->nrot, (T *)h->d_rot_rec, h->stream)) return -1;
+            if ((h->g.flags & SESNT_FLAG_ROTATION) && o->rot_strain(a, nullptr, h->nel, (T *)h->rot_full, h->stream))
+                return -1;
             if (o->element(a, h->sls, h->aniso, h->stream)) return -1;
             cudaEventRecord(ev[1], h->stream);
             if (o->sources(a, h->stream)) return -1;
@@ -1125,7 +1367,10 @@ int sesnt_info(const sesnt_t *h, long long out[6]) {
     out[2] = h->nuni;
     out[3] = (long long)h->dev_bytes;
     out[4] = algorithmic_bytes(h->nloc, h->nuni, h->sls ? kNsls : 0, h->aniso, h->S, h->esize);
-    out[5] = 2 + (h->nsrc_rec > 0 || !h->sources.empty() ? 1 : 0) + (h->rec_elem.empty() ? 0 : 1);
+    bool rot_rec = false;
+    for (unsigned m : h->rec_mask) rot_rec = rot_rec || (m & (SESNT_CH_ROT_VX | SESNT_CH_ROT_VY | SESNT_CH_ROT_VZ));
+    out[5] = 2 + (h->nsrc_rec > 0 || !h->sources.empty() ? 1 : 0) + (h->rec_elem.empty() ? 0 : 1) + (rot_rec ? 1 : 0) +
+             ((h->g.flags & SESNT_FLAG_ROTATION) ? 1 : 0);
     return SESNT_OK;
 }
 
@@ -1136,5 +1381,121 @@ long long sesnt_footprint_bytes(const sesnt_grid_t *grid) {
 }
 
 void *sesnt_stream(const sesnt_t *h) { return h ? (void *)h->stream : nullptr; }
+
+int sesnt_get_trace(sesnt_t *h, int sim, int receiver, unsigned channel, float *out) {
+    if (!h || !out) return SESNT_EINVAL;
+    if (sim < 0 || sim >= h->S) return h->fail(SESNT_ERANGE, "simulation %d outside 0..%d", sim, h->S - 1);
+    if (receiver < 0 || receiver >= (int)h->rec_elem.size())
+        return h->fail(SESNT_ERANGE, "receiver %d outside 0..%d", receiver, (int)h->rec_elem.size() - 1);
+    if (channel == 0 || (channel & (channel - 1)) || channel > SESNT_CH_FZ)
+        return h->fail(SESNT_EINVAL, "channel must be one SESNT_CH_* bit");
+    if (!(h->rec_mask[receiver] & channel))
+        return h->fail(SESNT_EINVAL, "channel 0x%x was not requested for receiver %d", channel, receiver);
+    int rc;
+    if (h->rec_dirty) {
+        if ((rc = h->dbl ? upload_receivers<double>(h) : upload_receivers<float>(h))) return rc;
+        if ((rc = upload_receiver_sources(h))) return rc;
+    }
+    const size_t nt = h->g.nt, nrec = h->rec_elem.size(), E = h->esize;
+    const void *src;
+    double sign = 1.0;
+    if (channel <= SESNT_CH_N) {
+        const int c = channel == SESNT_CH_N ? 0 : __builtin_ctz(channel);
+        if (channel == SESNT_CH_N) sign = -1.0;  // record_n: SUM(-1.0*vanderm*vx)
+        src = (const char *)h->d_seis + (((size_t)sim * nrec + receiver) * 3 + c) * nt * E;
+    } else {
+        const unsigned xm = h->rec_mask[receiver] & kDeviceChannels;
+        const int slot = h->rec_xslot[receiver] + __builtin_popcount(xm & (channel - 1));
+        src = (const char *)h->d_xseis + ((size_t)sim * h->nxtr + slot) * nt * E;
+    }
+    std::vector<double> tmp(nt);
+    std::vector<float> tf(nt);
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e == cudaSuccess) e = cudaMemcpy(h->dbl ? (void *)tmp.data() : (void *)tf.data(), src, nt * E, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return h->cuda_fail(e, "reading trace");
+    if ((rc = h->wait_status())) return rc;
+    for (size_t t = 0; t < nt; ++t) out[t] = h->dbl ? (float)(sign * tmp[t]) : (float)(sign * tf[t]);
+    return SESNT_OK;
+}
+
+namespace {
+struct FieldName { int id; const char *name; };
+const FieldName kFieldNames[] = {
+    {SESNT_FIELD_VX, "vx"}, {SESNT_FIELD_VY, "vy"}, {SESNT_FIELD_VZ, "vz"},
+    {SESNT_FIELD_SXX, "sxx"}, {SESNT_FIELD_SXY, "sxy"}, {SESNT_FIELD_SXZ, "sxz"},
+    {SESNT_FIELD_SYY, "syy"}, {SESNT_FIELD_SYZ, "syz"}, {SESNT_FIELD_SZZ, "szz"},
+    {SESNT_FIELD_TAPER, "taper"}, {SESNT_FIELD_MASS, "mm"},
+    {SESNT_FIELD_PRESSURE, "pressure"},
+    {SESNT_FIELD_EXX, "exx"}, {SESNT_FIELD_EXY, "exy"}, {SESNT_FIELD_EXZ, "exz"},
+    {SESNT_FIELD_EYY, "eyy"}, {SESNT_FIELD_EYZ, "eyz"}, {SESNT_FIELD_EZZ, "ezz"},
+    {SESNT_FIELD_ROT_VX, "rot_vx"}, {SESNT_FIELD_ROT_VY, "rot_vy"}, {SESNT_FIELD_ROT_VZ, "rot_vz"},
+    {SESNT_FIELD_LAMBDA, "lambda"}, {SESNT_FIELD_MU, "mu"},
+    {SESNT_FIELD_A, "a"}, {SESNT_FIELD_B, "b"}, {SESNT_FIELD_C, "c"}};
+}  // namespace
+
+const char *sesnt_field_name(int which) {
+    for (const auto &f : kFieldNames)
+        if (f.id == which) return f.name;
+    return nullptr;
+}
+
+int sesnt_field_id(const char *name) {
+    if (!name) return -1;
+    std::string n(name);
+    while (!n.empty() && (n.back() == ' ' || n.back() == '\t')) n.pop_back();
+    size_t b = 0;
+    while (b < n.size() && (n[b] == ' ' || n[b] == '\t')) ++b;
+    n = n.substr(b);
+    for (auto &ch : n) ch = (char)std::tolower((unsigned char)ch);
+    for (const auto &f : kFieldNames)
+        if (n == f.name) return f.id;
+    return -1;
+}
+
+int sesnt_add_snapshot(sesnt_t *h, int sim, int which, int ts_start, int ts_increment, int ts_end,
+                       const char *prefix, const char *attribute, int override) {
+    if (!h) return SESNT_EINVAL;
+    if (sim < 0 || sim >= h->S) return h->fail(SESNT_ERANGE, "simulation %d outside 0..%d", sim, h->S - 1);
+    const char *name = sesnt_field_name(which);
+    if (!name || which == SESNT_FIELD_MASS) return h->fail(SESNT_EINVAL, "field %d cannot be snapshotted", which);
+    if (which >= SESNT_FIELD_EXX && which <= SESNT_FIELD_EZZ && !h->du)
+        return h->fail(SESNT_ESTATE, "strain snapshots need SESNT_FLAG_STRAIN at sesnt_create");
+    if (ts_end <= 0) ts_end = h->g.nt;
+    // range checks of volume_snapshot_cls' constructor (src/volume_snapshot.f90:71-113)
+    if (ts_start < 1) return h->fail(SESNT_ERANGE, "timestep_start out of range");
+    if (ts_increment < 1 || ts_increment > h->g.nt) return h->fail(SESNT_ERANGE, "timestep_increment out of range");
+    if (ts_end < ts_start) return h->fail(SESNT_ERANGE, "timestep_end out of range");
+    int rc;
+    const size_t bytes = (size_t)h->nloc * h->esize;
+    if (!h->writer) h->writer.reset(new SnapshotWriter());
+    std::string err;
+    if ((rc = h->writer->start(h->device, bytes, 3, err))) return h->fail(rc, "%s", err.c_str());
+    if (!h->snap_stage && (rc = h->alloc(&h->snap_stage, bytes, "snapshot staging"))) return rc;
+    if (is_rotation(which) && !h->rot_full &&
+        (rc = h->alloc(&h->rot_full, 6 * bytes * h->S, "rotation strain")))
+        return rc;
+    sesnt_handle::Snapshot q;
+    q.sim = sim;
+    q.which = which;
+    q.start = ts_start;
+    q.inc = ts_increment;
+    q.end = ts_end;
+    q.prefix = (prefix && *prefix) ? prefix : "./";
+    q.attribute = attribute ? attribute : name;
+    q.override = override != 0;
+    h->snaps.push_back(q);
+    return (int)h->snaps.size() - 1;
+}
+
+int sesnt_snapshots_wait(sesnt_t *h) {
+    if (!h) return SESNT_EINVAL;
+    if (!h->writer) return SESNT_OK;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "synchronize");
+    std::string err;
+    const int rc = h->writer->wait(err);
+    if (rc) return h->fail(rc, "%s", err.c_str());
+    return SESNT_OK;
+}
 
 }  // extern "C"

@@ -81,7 +81,25 @@ struct StepArgs {
     int contraction; // element kernel contractions: 0 CUDA cores, 1 tensor cores TF32x3, 2 tensor cores BF16x3
     T two_over_d[3]; // 2/dx_elm, 2/dy_elm, 2/dz_elm
     int *err;        // device error word (a bounded wait ran out)
+    // displacement gradient [S][9][nloc] (order kDu*), or null when not kept
+    T *du;
+    // receiver channels beyond vx, vy, vz (SESNT_CH_ROT_* , _M**, _F*):
+    // per receiver the device-computed channel bits and its first trace slot;
+    // the rotation-strain slot of its element (or -1); per (sim, receiver)
+    // the source record of the receiver's element (or -1)
+    const unsigned *rec_xmask;
+    const int *rec_xslot, *rec_rot, *rec_src;
+    T *xseis;            // [S][nxtr][nt]
+    const T *rot_rec;    // [S][6][nrot][NP] rotation strain of the receiver elements
+    int nxtr, nrot;
 };
+
+// Displacement-gradient components (src/evolution.f90:179-187).
+enum { kDuXX = 0, kDuYY, kDuZZ, kDuXY, kDuYX, kDuXZ, kDuZX, kDuYZ, kDuZY };
+// Rotation strain: the gradient components the reference's rot_v channels
+// read after a step (src/config/channel_mod.f90:620-812), i.e. the completed
+// gradient with exy, exz, eyz already symmetrised (src/evolution.f90:206-208).
+enum { kRotEYZ = 0, kRotEZY, kRotEZX, kRotEXZ, kRotEXY, kRotEYX };
 
 // Kernel launchers for one polynomial degree and one precision, filled in by
 // the per-degree translation units.
@@ -101,6 +119,13 @@ struct LpdOps {
     int (*scatter_unique)(const StepArgs<T> &, const T *loc, T *uni, void *stream);
     // element-local taper (for get_field).
     int (*taper_local)(const StepArgs<T> &, T *loc, void *stream);
+    // rotation strain of `count` elements (elems, or all elements when null)
+    // from the current velocity: out[((s*6 + c)*count + idx)*NP + p].
+    int (*rot_strain)(const StepArgs<T> &, const int *elems, int count, T *out, void *stream);
+    // element-local derived field of simulation `sim`: SESNT_FIELD_PRESSURE,
+    // _EXX.._EZZ (from du), _ROT_VX.._ROT_VZ (from the full-volume rotation
+    // strain `rot` [S][6][nloc] and the current velocity).
+    int (*derived)(const StepArgs<T> &, int which, int sim, const T *rot, T *loc, void *stream);
     // one-time kernel attributes (large dynamic shared memory)
     int (*prepare)();
     int threads_element;

@@ -29,11 +29,23 @@ FLAG_NO_GRAPH = 2
 FLAG_PERSISTENT_ELEMENT = 4
 FLAG_TC_TF32X3 = 8
 FLAG_TC_BF16X3 = 16
+FLAG_STRAIN = 32
+FLAG_ROTATION = 64
 SOURCE_MT, SOURCE_SF = 0, 1
 WAVELETS = {"DELTA": 0, "RICKER": 1, "GAUSS": 2, "SIN**3": 3, "BRUNE": 4}
-CH_VX, CH_VY, CH_VZ = 1, 2, 4
+CH_VX, CH_VY, CH_VZ, CH_N = 1, 2, 4, 8
+CH_ROT_VX, CH_ROT_VY, CH_ROT_VZ = 16, 32, 64
+CH_MXX, CH_MXY, CH_MXZ, CH_MYY, CH_MYZ, CH_MZZ = 128, 256, 512, 1024, 2048, 4096
+CH_FX, CH_FY, CH_FZ = 8192, 16384, 32768
+# receiver attributes of the reference (construct_channel_container_receiver)
+CHANNELS = {"vx": CH_VX, "vy": CH_VY, "e": CH_VY, "vz": CH_VZ, "z": CH_VZ, "n": CH_N,
+            "rot_vx": CH_ROT_VX, "rot_vy": CH_ROT_VY, "rot_vz": CH_ROT_VZ,
+            "mxx": CH_MXX, "mxy": CH_MXY, "myx": CH_MXY, "mxz": CH_MXZ, "mzx": CH_MXZ, "myy": CH_MYY,
+            "myz": CH_MYZ, "mzy": CH_MYZ, "mzz": CH_MZZ, "fx": CH_FX, "fy": CH_FY, "fz": CH_FZ}
 FIELDS = {"vx": 0, "vy": 1, "vz": 2, "sxx": 3, "sxy": 4, "sxz": 5, "syy": 6, "syz": 7, "szz": 8,
-          "taper": 9, "mass": 10}
+          "taper": 9, "mass": 10, "pressure": 40, "exx": 41, "exy": 42, "exz": 43, "eyy": 44, "eyz": 45,
+          "ezz": 46, "rot_vx": 47, "rot_vy": 48, "rot_vz": 49, "lambda": 50, "mu": 51, "a": 52, "b": 53,
+          "c": 54}
 MEMORY_FIELD0 = 13
 
 
@@ -163,6 +175,11 @@ def lib():
         "sesnt_config_get": (I, [P, C.c_char_p, I, C.c_char_p, C.c_char_p, I]),
         "sesnt_config_json": (I, [P, C.c_char_p, C.c_longlong, C.POINTER(C.c_longlong)]),
         "sesnt_forward": (I, [C.c_char_p, I, C.POINTER(C.c_int)]),
+        "sesnt_get_trace": (I, [P, I, I, U, fp]),
+        "sesnt_add_snapshot": (I, [P, I, I, I, I, I, C.c_char_p, C.c_char_p, I]),
+        "sesnt_snapshots_wait": (I, [P]),
+        "sesnt_field_name": (C.c_char_p, [I]),
+        "sesnt_field_id": (I, [C.c_char_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -302,6 +319,25 @@ class Simulation:
         if self.receivers:
             self._c(lib().sesnt_get_seismograms(self._h, _fptr(out)))
         return out
+
+    def trace(self, receiver, channel, sim=0):
+        """One receiver channel (CH_* bit or attribute name), float32 [nt]."""
+        ch = CHANNELS[channel] if isinstance(channel, str) else int(channel)
+        out = np.zeros(self.grid.nt, np.float32)
+        self._c(lib().sesnt_get_trace(self._h, sim, receiver, ch, _fptr(out)))
+        return out
+
+    def add_snapshot(self, field, start, increment, end=0, prefix="./", attribute=None, sim=0, override=False):
+        """Volume snapshot of `field` (name or FIELD code) written to
+        <prefix><attribute>_<it>.vol after every due step (written by a
+        background thread; wait_snapshots() waits for the files)."""
+        code = FIELDS[field] if isinstance(field, str) else int(field)
+        return self._c(lib().sesnt_add_snapshot(self._h, sim, code, start, increment, end,
+                                                prefix.encode() if prefix else None,
+                                                attribute.encode() if attribute else None, 1 if override else 0))
+
+    def wait_snapshots(self):
+        self._c(lib().sesnt_snapshots_wait(self._h))
 
     def field(self, which, sim=0, precision=4):
         code = FIELDS[which] if isinstance(which, str) else int(which)

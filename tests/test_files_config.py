@@ -168,3 +168,56 @@ def test_forward_from_config_file(gpu, sesnt_lib, oracle_mod, tmp_path, monkeypa
             data = np.fromfile("%s.%s.%s.%s.sac" % (net, sta, loc, ch), "<f4")[158:]
             c = "xyz".index(ch[1])
             assert np.linalg.norm(data - ref[r, c]) / scale < 1e-4, (sta, ch)
+
+
+@pytest.mark.gpu
+def test_forward_channels_and_raw_snapshots(gpu, sesnt_lib, oracle_mod, tmp_path, monkeypatch):
+    """Receiver attributes beyond vx/vy/vz ('n', 'e', 'z', 'rot_vz', an
+    unknown one that is dropped) and &output_raw snapshots of a wavefield, a
+    rotation, a strain and a model attribute, from a config file."""
+    nt = 120
+    wl = workloads.config1(nt=nt)
+    g = wl.grid
+    monkeypatch.chdir(tmp_path)
+    for key in ("rhoinv", "lambda", "mu"):
+        sesnt.write_raw_field(key, g, wl.model[key])
+    text = open(os.path.join(CONFIGS, "plain_12x12x8.conf")).read().replace("nt = 2000", "nt = %d" % nt)
+    text = text.replace("attributes = 'vx', 'vy', 'vz'", "attributes = 'n', 'e', 'z', 'rot_vz', 'bogus'")
+    os.mkdir("snap")
+    text += """
+&output_raw
+    timestep_start = 30
+    timestep_increment = 45
+    attributes = 'vz' 'rot_vz' 'exx' 'rho'
+    prefix = './snap/'
+/
+"""
+    (tmp_path / "config").write_text(text)
+    assert sesnt.forward("config") == 4 + 2 + 1
+    for ch in ("n", "e", "z", "rot_vz"):
+        assert os.path.exists("GB.R01.00.%s.sac" % ch)
+    n = np.fromfile("GB.R01.00.n.sac", "<f4")[158:]
+    o = oracle_mod.Oracle(g)
+    rec = [(35.5, 10.0, 0.0), (38.5, 10.0, 0.0), (41.5, 10.0, 1000.0)]
+    masks = [sesnt.CH_VX | sesnt.CH_VY | sesnt.CH_VZ | sesnt.CH_N | sesnt.CH_ROT_VZ, 7, 7]
+    o.keep_strain()
+    oracle_mod.load_workload(o, workloads.Workload("c", g, wl.model, wl.sources,
+                                                   [workloads.Receiver(*r) for r in rec]), masks=masks)
+    done = 0
+    for it in (30, 75, 120):
+        o.run(it - done)
+        done = it
+        for attr, code in (("vz", 2), ("rot_vz", 49), ("exx", 41)):
+            got = sesnt.read_raw_field("snap/%s_%d.vol" % (attr, it), g)
+            want = o.field(code)
+            assert np.linalg.norm(got - want) / np.linalg.norm(want) < 1e-4, (attr, it)
+        rho = sesnt.read_raw_field("snap/rho_%d.vol" % it, g)
+        assert np.array_equal(rho, (np.float32(1) / wl.model["rhoinv"]).astype(np.float32))
+    assert sorted(os.listdir("snap")) == sorted("%s_%d.vol" % (a, it) for a in ("vz", "rot_vz", "exx", "rho")
+                                                for it in (30, 75, 120))
+    scale = np.linalg.norm(o.seismograms()[0])
+    assert np.linalg.norm(n - o.trace(0, sesnt.CH_N)) / scale < 1e-4
+    rz = np.fromfile("GB.R01.00.rot_vz.sac", "<f4")[158:]
+    want = o.trace(0, sesnt.CH_ROT_VZ)
+    assert np.linalg.norm(rz - want) / np.linalg.norm(want) < 1e-4
+    o.close()

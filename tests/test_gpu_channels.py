@@ -7,10 +7,11 @@ the oracle (the reference's channel classes and get_field restated):
   fields;
 - snapshots written behind the steps to <prefix><attribute>_<it>.vol.
 
-Tolerances: FP64 GPU against the FP64 oracle 1e-9 relative L2 (same
-algorithm, different summation order); FP32 against the FP32 oracle 1e-4
-relative to the field's (or trace's) norm; snapshot files (float32) against
-the FP64 oracle within float32 rounding (1e-6).
+Tolerances: FP64 fields against the FP64 oracle 1e-9 relative L2 (same
+algorithm, different summation order); FP64 traces within float32 rounding
+(1e-6: traces are returned as float32, like the reference's REAL32 channel
+data); FP32 against the FP32 oracle 1e-4 relative to the field's (or
+trace's) norm; snapshot files (float32) against the FP64 oracle 1e-6.
 """
 import os
 
@@ -105,7 +106,7 @@ def compare_traces(got, want, tol):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision,tol", [(8, 1e-9), (4, 1e-4)])
+@pytest.mark.parametrize("precision,tol", [(8, 1e-6), (4, 1e-4)])
 def test_rotation_and_n_channels(gpu, sesnt_lib, oracle_mod, precision, tol):
     wl = with_grid(channel_workload(n_sls=3), precision=precision)
     masks = masks_for(wl, ROT | sesnt.CH_N)
@@ -127,7 +128,7 @@ def test_recorded_source_channels(gpu, sesnt_lib, oracle_mod, kind, bits):
     want, _ = oracle_traces(oracle_mod, wl, masks, 120, 8)
     # receiver 0 is in the source element and sees the slab; the others see zero
     assert max(np.abs(want[(0, b)]).max() for b in (1 << q for q in range(16)) if bits & b) > 0
-    compare_traces(got, want, 1e-9)
+    compare_traces(got, want, 1e-6)
 
 
 @pytest.mark.gpu

@@ -220,8 +220,18 @@ int sesnt_run_profiled(sesnt_t *h, int it0, int nsteps, float ms[4]);
 /* Waits for all work queued on the handle. */
 int sesnt_synchronize(sesnt_t *h);
 
-/* Zeroes the wavefield, memory variables and seismograms (model kept). */
+/* Zeroes the wavefield, memory variables and seismograms (model kept) and
+ * clears the error word of an earlier SESNT_ETIMEOUT. */
 int sesnt_reset(sesnt_t *h);
+
+/* No counterpart in the reference. Failure-detection hook: every device-side
+ * completion wait (the tensor-core element kernel's mbarrier waits) gives up
+ * after `polls` polls (default 4,194,304), sets the handle's error word and
+ * leaves the state of its points unchanged; the next synchronising call then
+ * returns SESNT_ETIMEOUT until sesnt_reset. drop_completion != 0 makes that
+ * kernel signal no completion, so its waits run out: a test of the path
+ * that faults nothing. */
+int sesnt_set_wait_limit(sesnt_t *h, int polls, int drop_completion);
 
 /* Seismograms, float32 [batch][nrec][3][nt] with components vx, vy, vz
  * (channels not requested at sesnt_add_receiver are zero). Synchronous. */

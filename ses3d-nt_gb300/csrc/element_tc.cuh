@@ -80,10 +80,11 @@ __device__ __forceinline__ void tc_split_store(unsigned char *hi, unsigned char 
     }
 }
 
-// Bounded wait for the mbarrier phase `parity`; false when it ran out.
-__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
+// Bounded wait for the mbarrier phase `parity` (at most `polls` polls);
+// false when it ran out.
+__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity, int polls) {
     uint32_t done = 0;
-    for (int it = 0; it < (1 << 22) && !done; ++it)
+    for (int it = 0; it < polls && !done; ++it)
         asm volatile(
             "{.reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p;}"
             : "=r"(done)
@@ -245,14 +246,14 @@ __global__ void __launch_bounds__(TcCfg<N, PREC>::NT) k_element_tc(const StepArg
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
-    if (t == 0) tc_issue<PREC, C::TILES>(tmem, 0, a_hi, a_lo, bg_hi, bg_lo, smem_addr(mbar));
+    if (t == 0 && !a.drop_completion) tc_issue<PREC, C::TILES>(tmem, 0, a_hi, a_lo, bg_hi, bg_lo, smem_addr(mbar));
     // block-uniform outcome: tcgen05.ld below is warp-collective
-    const bool ok1 = __syncthreads_and(tc_wait(smem_addr(mbar), 0)) != 0;
+    const bool ok1 = __syncthreads_and(tc_wait(smem_addr(mbar), 0, a.wait_polls)) != 0;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const float gscale[3] = {a.two_over_d[0], a.two_over_d[1], a.two_over_d[2]};
     if (ok1) tc_read_rows<N, PREC>(tmem, 0, slab, gscale);
     __syncthreads();
-    if (act) {
+    if (act && ok1) {  // without the gradient the point keeps its state
         T ev[9];
         // slab[(d*3 + c)*NP + p] = d-derivative of component c: the layout of strain_contract
 #pragma unroll
@@ -271,7 +272,7 @@ __global__ void __launch_bounds__(TcCfg<N, PREC>::NT) k_element_tc(const StepArg
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (t == 0 && ok1) tc_issue<PREC, C::TILES>(tmem, C::COLS_PER_PASS, a_hi, a_lo, bd_hi, bd_lo, smem_addr(mbar));
-    const bool ok = __syncthreads_and(ok1 && tc_wait(smem_addr(mbar), 1)) != 0;
+    const bool ok = __syncthreads_and(ok1 && tc_wait(smem_addr(mbar), 1, a.wait_polls)) != 0;
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const float one[3] = {1.0f, 1.0f, 1.0f};
     if (ok) tc_read_rows<N, PREC>(tmem, C::COLS_PER_PASS, slab, one);
@@ -280,7 +281,7 @@ __global__ void __launch_bounds__(TcCfg<N, PREC>::NT) k_element_tc(const StepArg
         // record the failure; give the products still in flight one more
         // bounded wait before the accumulator columns are freed
         if (t == 0) atomicExch(a.err, 1);
-        tc_wait(smem_addr(mbar), ok1 ? 1u : 0u);
+        tc_wait(smem_addr(mbar), ok1 ? 1u : 0u, a.wait_polls);
     }
     if (act && ok) {
         // slab[(d*3 + c)*NP + p]: direction-d part of force component c

@@ -148,6 +148,7 @@ struct sesnt_handle {
     void *sig = nullptr, *mem = nullptr, *v = nullptr, *vc = nullptr, *F = nullptr, *invM = nullptr;
     int *d_it = nullptr;
     int *d_err = nullptr;  // set by a kernel whose bounded wait ran out
+    int wait_polls = 1 << 22, drop_completion = 0;
     double dt = 0, c1 = 0, c2 = 0, c3 = 0, jac = 0, alpha = 0, two_over_d[3] = {0, 0, 0};
     // sources and receivers
     std::vector<HostSource> sources;
@@ -281,6 +282,8 @@ struct sesnt_handle {
         a.two_over_d[1] = (T)two_over_d[1];
         a.two_over_d[2] = (T)two_over_d[2];
         a.err = d_err;
+        a.wait_polls = wait_polls;
+        a.drop_completion = drop_completion;
         a.du = (T *)du;
         a.rec_xmask = nxtr > 0 ? d_rec_xmask : nullptr;
         a.rec_xslot = d_rec_xslot; a.rec_rot = d_rec_rot; a.rec_src = d_rec_src;
@@ -1331,7 +1334,18 @@ int sesnt_reset(sesnt_t *h) {
     if (!h) return SESNT_EINVAL;
     int rc = zero_state(h);
     if (rc) return rc;
+    cudaError_t e = cudaMemsetAsync(h->d_err, 0, sizeof(int), h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "clearing the error word");
     return sesnt_synchronize(h);
+}
+
+int sesnt_set_wait_limit(sesnt_t *h, int polls, int drop_completion) {
+    if (!h) return SESNT_EINVAL;
+    if (polls < 1) return h->fail(SESNT_EINVAL, "polls must be >= 1");
+    h->drop_graph();  // the limit is a launch argument captured in the graph
+    h->wait_polls = polls;
+    h->drop_completion = drop_completion ? 1 : 0;
+    return SESNT_OK;
 }
 
 int sesnt_get_seismograms(sesnt_t *h, float *out) {

@@ -81,6 +81,8 @@ struct StepArgs {
     int contraction; // element kernel contractions: 0 CUDA cores, 1 tensor cores TF32x3, 2 tensor cores BF16x3
     T two_over_d[3]; // 2/dx_elm, 2/dy_elm, 2/dz_elm
     int *err;        // device error word (a bounded wait ran out)
+    int wait_polls;  // bound of every device-side completion wait (mbarrier polls)
+    int drop_completion;  // failure-detection test hook: the tensor-core kernel signals no completion
     // displacement gradient [S][9][nloc] (order kDu*), or null when not kept
     T *du;
     // receiver channels beyond vx, vy, vz (SESNT_CH_ROT_* , _M**, _F*):

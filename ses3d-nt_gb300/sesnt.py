@@ -176,6 +176,7 @@ def lib():
         "sesnt_config_json": (I, [P, C.c_char_p, C.c_longlong, C.POINTER(C.c_longlong)]),
         "sesnt_forward": (I, [C.c_char_p, I, C.POINTER(C.c_int)]),
         "sesnt_get_trace": (I, [P, I, I, U, fp]),
+        "sesnt_set_wait_limit": (I, [P, I, I]),
         "sesnt_add_snapshot": (I, [P, I, I, I, I, I, C.c_char_p, C.c_char_p, I]),
         "sesnt_snapshots_wait": (I, [P]),
         "sesnt_field_name": (C.c_char_p, [I]),
@@ -310,6 +311,9 @@ class Simulation:
 
     def synchronize(self):
         self._c(lib().sesnt_synchronize(self._h))
+
+    def set_wait_limit(self, polls, drop_completion=False):
+        self._c(lib().sesnt_set_wait_limit(self._h, polls, 1 if drop_completion else 0))
 
     def reset(self):
         self._c(lib().sesnt_reset(self._h))

@@ -85,3 +85,29 @@ def test_tensor_core_batch_and_graph(gpu, sesnt_lib):
         one.sources[0].sim = 0
         os_, _, _ = run_gpu(one, 100, fields=())
         assert rel_l2(gs[s], os_[0]) < 1e-5
+
+
+@pytest.mark.gpu
+def test_completion_wait_runs_out_and_reports(gpu, sesnt_lib):
+    """Failure detection without a fault: with the completion signal dropped
+    the kernel's bounded mbarrier waits run out, the error word is set and
+    synchronising returns SESNT_ETIMEOUT; after sesnt_reset the handle steps
+    normally again."""
+    wl = small_workload(4, nt=40)
+    g = with_grid(wl, flags=sesnt.FLAG_TC_TF32X3)
+    with sesnt.Simulation(g.grid) as sim:
+        workloads.setup(sim, g)
+        sim.set_wait_limit(64, drop_completion=True)
+        sim.run(1, 2)
+        with pytest.raises(sesnt.SesntError) as e:
+            sim.synchronize()
+        assert e.value.code == sesnt.ETIMEOUT
+        with pytest.raises(sesnt.SesntError) as e:
+            sim.seismograms()
+        assert e.value.code == sesnt.ETIMEOUT
+        sim.set_wait_limit(1 << 22)
+        sim.reset()
+        sim.run(1, 40)
+        again = sim.seismograms()
+    fresh, _, _ = run_gpu(g, 40, fields=())
+    assert rel_l2(again, fresh) < 1e-6

@@ -259,7 +259,7 @@ __global__ void __launch_bounds__(TcCfg<N, PREC>::NT) k_element_tc(const StepArg
 #pragma unroll
         for (int q = 0; q < 9; ++q) ev[q] = slab[q * NP + p];
         point_update<N, T, NSLS, ANISO>(a, ev, vx, vy, vz, p, i, j, k, ex, ey, ez, lam, mu, tau, cA, cB, cC, sg, m,
-                                        sig, mem, nloc, slab, a.du ? a.du + (size_t)s * 9 * nloc + li : nullptr);
+                                        sig, mem, nloc, slab, nullptr);
         // fluxes slab[(c*3 + d)*NP + p] (force component c, direction d) into the divergence operand
 #pragma unroll
         for (int c = 0; c < 3; ++c) {

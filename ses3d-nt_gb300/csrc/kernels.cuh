@@ -161,9 +161,10 @@ __device__ __forceinline__ void complete_gradient(const StepArgs<T> &a, const T 
 }
 
 // The rest of one element-local point's step, from its raw velocity gradient
-// e[9] (layout of strain_contract) and velocity. du: this point's
-// displacement gradient (stride nloc) or null.
-template <int N, typename T, int NSLS, bool ANISO>
+// e[9] (layout of strain_contract) and velocity. DU: integrate this point's
+// displacement gradient `du` (stride nloc); a compile-time switch, since even
+// a skipped branch measured 1.5% on the step.
+template <int N, typename T, int NSLS, bool ANISO, bool DU = false>
 __device__ __forceinline__ void point_update(const StepArgs<T> &a, const T (&e)[9], T vx, T vy, T vz, int p, int i,
                                              int j, int k, int ex, int ey, int ez, T lam, T mu, T tau, T cA, T cB,
                                              T cC, const T (&sg)[6], const T (&m)[6][NSLS > 0 ? NSLS : 1], T *sig,
@@ -175,7 +176,7 @@ __device__ __forceinline__ void point_update(const StepArgs<T> &a, const T (&e)[
       ezx = g[kDuZX], eyz = g[kDuYZ], ezy = g[kDuZY];
     const T rr = a.r[ez * P + k];
     const T rs = rr * a.sin_t[ex * P + i];
-    if (du) {
+    if constexpr (DU) {
         // displacement gradient du += dt * (completed velocity gradient)
         // before the symmetrisation (src/evolution.f90:179-187)
 #pragma unroll
@@ -268,7 +269,7 @@ __device__ __forceinline__ void point_update(const StepArgs<T> &a, const T (&e)[
 }
 
 // One element-local point of the step with CUDA-core contractions.
-template <int N, typename T, int NSLS, bool ANISO>
+template <int N, typename T, int NSLS, bool ANISO, bool DU = false>
 __device__ __forceinline__ void point_step(const StepArgs<T> &a, const T *sD, const T *svx, const T *svy,
                                            const T *svz, int p, int i, int j, int k, int ex, int ey, int ez,
                                            T lam, T mu, T tau, T cA, T cB, T cC, const T (&sg)[6],
@@ -276,8 +277,8 @@ __device__ __forceinline__ void point_step(const StepArgs<T> &a, const T *sD, co
                                            T *my, T *du) {
     T e[9];
     strain_contract<N, T>(sD, svx, svy, svz, i, j, k, e);
-    point_update<N, T, NSLS, ANISO>(a, e, svx[p], svy[p], svz[p], p, i, j, k, ex, ey, ez, lam, mu, tau, cA, cB, cC,
-                                    sg, m, sig, mem, nloc, my, du);
+    point_update<N, T, NSLS, ANISO, DU>(a, e, svx[p], svy[p], svz[p], p, i, j, k, ex, ey, ez, lam, mu, tau, cA, cB,
+                                        cC, sg, m, sig, mem, nloc, my, du);
 }
 
 // Weak divergence at point (i,j,k): transposed line contractions over the
@@ -304,7 +305,7 @@ __device__ __forceinline__ size_t unique_index(int NXU, int NYU, int ex, int ey,
 }
 
 // One block per group of EPB elements and simulation.
-template <int N, typename T, int NSLS, bool ANISO>
+template <int N, typename T, int NSLS, bool ANISO, bool DU>
 __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::MINB : 1) k_element(const StepArgs<T> a) {
     constexpr int P = ElemCfg<N>::P, NP = ElemCfg<N>::NP, EPB = ElemCfg<N>::EPB, NT = ElemCfg<N>::NT;
     constexpr int MS = NSLS > 0 ? NSLS : 1;
@@ -366,9 +367,9 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::M
     __syncthreads();
     if (act) {
         const T *svx = sv + le * 3 * NP;
-        point_step<N, T, NSLS, ANISO>(a, sD, svx, svx + NP, svx + 2 * NP, p, i, j, k, ex, ey, ez, lam, mu, tau, cA,
-                                      cB, cC, sg, m, sig, mem, nloc, sf + le * 9 * NP,
-                                      a.du ? a.du + (size_t)s * 9 * nloc + li : nullptr);
+        point_step<N, T, NSLS, ANISO, DU>(a, sD, svx, svx + NP, svx + 2 * NP, p, i, j, k, ex, ey, ez, lam, mu, tau,
+                                          cA, cB, cC, sg, m, sig, mem, nloc, sf + le * 9 * NP,
+                                          DU ? a.du + (size_t)s * 9 * nloc + li : nullptr);
     }
     __syncthreads();
     if (act) {
@@ -532,8 +533,7 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT) k_element_pf(const StepArgs<T>
             const T *svx = svb + b * 3 * SLAB + le * NP;
             point_step<N, T, NSLS, ANISO>(a, sD, svx, svx + SLAB, svx + 2 * SLAB, p, i, j, k, ex, ey, ez, lam, mu,
                                           tau, cA, cB, cC, sg, m, a.sig + (size_t)s * 6 * nloc + li,
-                                          a.mem + (size_t)s * 6 * MS * nloc + li, nloc, sf + le * 9 * NP,
-                                          a.du ? a.du + (size_t)s * 9 * nloc + li : nullptr);
+                                          a.mem + (size_t)s * 6 * MS * nloc + li, nloc, sf + le * 9 * NP, nullptr);
         }
         __syncthreads();  // fluxes complete; buffer b free for the group after next
         if (idx + 2 * stride < ngroups) prefetch(b, idx + 2 * stride);
@@ -829,7 +829,8 @@ int launch_element_v(const StepArgs<T> &a, void *stream) {
         k_element_pf<N, T, NSLS, ANISO><<<(unsigned)blocks, C::NT, PF::SMEM, (cudaStream_t)stream>>>(a);
     } else {
         const size_t smem = sizeof(T) * (4 * C::P * C::P + C::EPB * 12 * C::NP);
-        k_element<N, T, NSLS, ANISO><<<(unsigned)groups, C::NT, smem, (cudaStream_t)stream>>>(a);
+        if (a.du) k_element<N, T, NSLS, ANISO, true><<<(unsigned)groups, C::NT, smem, (cudaStream_t)stream>>>(a);
+        else k_element<N, T, NSLS, ANISO, false><<<(unsigned)groups, C::NT, smem, (cudaStream_t)stream>>>(a);
     }
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
@@ -842,7 +843,11 @@ int prepare_variant() {
     const size_t smem = sizeof(T) * (4 * C::P * C::P + C::EPB * 12 * C::NP);
     cudaError_t e = cudaSuccess;
     if (smem > 48 * 1024)
-        e = cudaFuncSetAttribute(k_element<N, T, NSLS, ANISO>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = cudaFuncSetAttribute(k_element<N, T, NSLS, ANISO, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
+    if (e == cudaSuccess && smem > 48 * 1024)
+        e = cudaFuncSetAttribute(k_element<N, T, NSLS, ANISO, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem);
     if (e == cudaSuccess && PF::SMEM <= kMaxSmemPerBlock) {
         e = cudaFuncSetAttribute(k_element_pf<N, T, NSLS, ANISO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)PF::SMEM);

@@ -136,6 +136,10 @@ struct sesnt_handle {
     bool dbl = false, sls = false, aniso = false, kahan = false, use_graph = true, model_set = false;
     int esize = 4;
     cudaStream_t stream = nullptr;
+    // second stream for the small per-step kernels (sources, receivers),
+    // forked from and joined back into `stream` within every enqueue
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_src = nullptr, ev_node = nullptr, ev_join = nullptr;
     std::string err;
     std::vector<DevBuf> bufs;
     size_t dev_bytes = 0;
@@ -251,6 +255,9 @@ struct sesnt_handle {
         for (auto &b : bufs) cudaFree(b.p);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
+        for (cudaEvent_t ev : {ev_fork, ev_src, ev_node, ev_join})
+            if (ev) cudaEventDestroy(ev);
+        if (side) cudaStreamDestroy(side);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -335,6 +342,11 @@ int check_grid(const sesnt_grid_t *g, std::string &why) {
         return bad("choose one tensor-core contraction mode");
     if ((g->flags & (SESNT_FLAG_TC_TF32X3 | SESNT_FLAG_TC_BF16X3)) && g->precision != 4) {
         why = "tensor-core contractions are built for FP32 wavefields only";
+        return SESNT_EUNSUPPORTED;
+    }
+    if ((g->flags & SESNT_FLAG_STRAIN) &&
+        (g->flags & (SESNT_FLAG_TC_TF32X3 | SESNT_FLAG_TC_BF16X3 | SESNT_FLAG_PERSISTENT_ELEMENT))) {
+        why = "the displacement gradient is built into the default element kernel only";
         return SESNT_EUNSUPPORTED;
     }
     if (g->batch < 1) return bad("batch must be >= 1");
@@ -634,25 +646,48 @@ int prepare_run(sesnt_t *h) {
     return SESNT_OK;
 }
 
-// Enqueue steps [it, it+n) given that *d_it == it: element, sources, node,
-// receivers per step.
+// Enqueue steps [it, it+n) given that *d_it == it. Per step:
+//   main:  [whole-volume rotation strain]  element ............ node
+//   side:  [receiver rotation strain]  sources ........ ^        `-> receivers
+// The source slab only adds into the force that the element kernel also adds
+// into, so it runs beside it; the receivers of step it read the velocity the
+// element kernel of step it+1 only reads, so they overlap that launch. The
+// node kernel waits for the side stream's sources (and, through the side
+// stream's order, the previous receivers). Side is joined back into main at
+// the end, also inside a graph capture.
 template <typename T>
 int enqueue_steps(sesnt_t *h, int n, bool rot_full = false) {
     const LpdOps<T> *o = ops<T>(h);
     StepArgs<T> a = h->args<T>();
     rot_full = rot_full || (h->g.flags & SESNT_FLAG_ROTATION);
+    auto launch_fail = [&](const char *what) {
+        return h->fail(SESNT_ECUDA, "%s kernel launch failed: %s", what, cudaGetErrorString(cudaGetLastError()));
+    };
+    cudaError_t e = cudaSuccess;
     for (int q = 0; q < n; ++q) {
         a.step_off = q;
-        // rotation strain from the velocity before this step's update
-        if (h->nrot > 0 && o->rot_strain(a, h->d_rot_elems, h->nrot, (T *)h->d_rot_rec, h->stream))
-            return h->fail(SESNT_ECUDA, "rotation-strain kernel launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+        if ((e = cudaEventRecord(h->ev_fork, h->stream)) != cudaSuccess ||
+            (e = cudaStreamWaitEvent(h->side, h->ev_fork, 0)) != cudaSuccess)
+            return h->cuda_fail(e, "fork");
+        // rotation strain of the receivers' elements from the velocity before this step's update
+        if (h->nrot > 0 && o->rot_strain(a, h->d_rot_elems, h->nrot, (T *)h->d_rot_rec, h->side))
+            return launch_fail("rotation-strain");
+        if (o->sources(a, h->side)) return launch_fail("source");
         if (rot_full && o->rot_strain(a, nullptr, h->nel, (T *)h->rot_full, h->stream))
-            return h->fail(SESNT_ECUDA, "rotation-strain kernel launch failed: %s", cudaGetErrorString(cudaGetLastError()));
-        if (o->element(a, h->sls, h->aniso, h->stream)) return h->fail(SESNT_ECUDA, "element kernel launch failed: %s", cudaGetErrorString(cudaGetLastError()));
-        if (o->sources(a, h->stream)) return h->fail(SESNT_ECUDA, "source kernel launch failed: %s", cudaGetErrorString(cudaGetLastError()));
-        if (o->node(a, h->kahan, h->stream)) return h->fail(SESNT_ECUDA, "node kernel launch failed: %s", cudaGetErrorString(cudaGetLastError()));
-        if (o->receivers(a, h->stream)) return h->fail(SESNT_ECUDA, "receiver kernel launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+            return launch_fail("rotation-strain");
+        if (o->element(a, h->sls, h->aniso, h->stream)) return launch_fail("element");
+        if ((e = cudaEventRecord(h->ev_src, h->side)) != cudaSuccess ||
+            (e = cudaStreamWaitEvent(h->stream, h->ev_src, 0)) != cudaSuccess)
+            return h->cuda_fail(e, "join before the node update");
+        if (o->node(a, h->kahan, h->stream)) return launch_fail("node");
+        if ((e = cudaEventRecord(h->ev_node, h->stream)) != cudaSuccess ||
+            (e = cudaStreamWaitEvent(h->side, h->ev_node, 0)) != cudaSuccess)
+            return h->cuda_fail(e, "fork after the node update");
+        if (o->receivers(a, h->side)) return launch_fail("receiver");
     }
+    if ((e = cudaEventRecord(h->ev_join, h->side)) != cudaSuccess ||
+        (e = cudaStreamWaitEvent(h->stream, h->ev_join, 0)) != cudaSuccess)
+        return h->cuda_fail(e, "join");
     return SESNT_OK;
 }
 
@@ -1069,6 +1104,14 @@ int sesnt_create(const sesnt_grid_t *grid, sesnt_t **out) {
     }
     cudaEventCreate(&h->ev0);
     cudaEventCreate(&h->ev1);
+    e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
+    for (cudaEvent_t *ev : {&h->ev_fork, &h->ev_src, &h->ev_node, &h->ev_join})
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        g_create_error = std::string("creating the side stream: ") + cudaGetErrorString(e);
+        return SESNT_ECUDA;
+    }
     const size_t E = h->esize, P = h->P, nloc = (size_t)h->nloc, nuni = (size_t)h->nuni, S = h->S;
     struct A { void **p; size_t n; const char *w; } allocs[] = {
         {&h->tabD, 4 * P * P * E, "tables"}, {&h->w, P * E, "weights"},

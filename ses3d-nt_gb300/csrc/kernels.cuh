@@ -168,7 +168,7 @@ template <int N, typename T, int NSLS, bool ANISO, bool DU = false>
 __device__ __forceinline__ void point_update(const StepArgs<T> &a, const T (&e)[9], T vx, T vy, T vz, int p, int i,
                                              int j, int k, int ex, int ey, int ez, T lam, T mu, T tau, T cA, T cB,
                                              T cC, const T (&sg)[6], const T (&m)[6][NSLS > 0 ? NSLS : 1], T *sig,
-                                             T *mem, size_t nloc, T *my, T *du) {
+                                             T *mem, size_t cs, size_t nloc, T *my, T *du) {
     constexpr int P = N + 1, NP = P * P * P;
     T g[9];
     complete_gradient<N, T>(a, e, vx, vy, vz, i, k, ex, ez, g);
@@ -235,11 +235,11 @@ __device__ __forceinline__ void point_update(const StepArgs<T> &a, const T (&e)[
     const T szz = sg[5] + a.dt * rzz;
     const T tp = taper_value(a.px[ex * P + i], a.py[ey * P + j], a.pz[ez * P + k], a.inv_alpha);
     st_stream(sig, sxx * tp);
-    st_stream(sig + nloc, sxy * tp);
-    st_stream(sig + 2 * nloc, sxz * tp);
-    st_stream(sig + 3 * nloc, syy * tp);
-    st_stream(sig + 4 * nloc, syz * tp);
-    st_stream(sig + 5 * nloc, szz * tp);
+    st_stream(sig + cs, sxy * tp);
+    st_stream(sig + 2 * cs, sxz * tp);
+    st_stream(sig + 3 * cs, syy * tp);
+    st_stream(sig + 4 * cs, syz * tp);
+    st_stream(sig + 5 * cs, szz * tp);
     if constexpr (NSLS > 0) {
         // memory variables after the update, driven by this step's rates:
         // M <- M*(1 - dt/tau_p) - tau*dt/(n*tau_p)*e
@@ -249,7 +249,7 @@ __device__ __forceinline__ void point_update(const StepArgs<T> &a, const T (&e)[
             const T drive = tau * a.mem_drive[q];
 #pragma unroll
             for (int c = 0; c < 6; ++c)
-                st_stream(mem + (size_t)(c * NSLS + q) * nloc, m[c][q] * a.mem_keep[q] - drive * er[c]);
+                st_stream(mem + (size_t)(c * NSLS + q) * cs, m[c][q] * a.mem_keep[q] - drive * er[c]);
         }
     }
     // metric-weighted stresses for the weak divergence
@@ -273,12 +273,12 @@ template <int N, typename T, int NSLS, bool ANISO, bool DU = false>
 __device__ __forceinline__ void point_step(const StepArgs<T> &a, const T *sD, const T *svx, const T *svy,
                                            const T *svz, int p, int i, int j, int k, int ex, int ey, int ez,
                                            T lam, T mu, T tau, T cA, T cB, T cC, const T (&sg)[6],
-                                           const T (&m)[6][NSLS > 0 ? NSLS : 1], T *sig, T *mem, size_t nloc,
-                                           T *my, T *du) {
+                                           const T (&m)[6][NSLS > 0 ? NSLS : 1], T *sig, T *mem, size_t cs,
+                                           size_t nloc, T *my, T *du) {
     T e[9];
     strain_contract<N, T>(sD, svx, svy, svz, i, j, k, e);
     point_update<N, T, NSLS, ANISO, DU>(a, e, svx[p], svy[p], svz[p], p, i, j, k, ex, ey, ez, lam, mu, tau, cA, cB,
-                                        cC, sg, m, sig, mem, nloc, my, du);
+                                        cC, sg, m, sig, mem, cs, nloc, my, du);
 }
 
 // Weak divergence at point (i,j,k): transposed line contractions over the
@@ -334,8 +334,10 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::M
     T lam = 0, mu = 0, tau = 0, cA = 0, cB = 0, cC = 0;
     T sg[6] = {0, 0, 0, 0, 0, 0};
     T m[6][MS];
-    T *sig = a.sig + (size_t)s * 6 * nloc + li;
-    T *mem = a.mem + (size_t)s * 6 * MS * nloc + li;
+    // stress and memory variables: element-blocked [e][s][comp][p]
+    const size_t sb = (size_t)e * S + s;
+    T *sig = a.sig + sb * 6 * NP + p;
+    T *mem = a.mem + sb * 6 * MS * NP + p;
     if (act) {
         ex = e % a.nx;
         ey = (e / a.nx) % a.ny;
@@ -351,13 +353,13 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::M
             cC = ld_stream(a.C + li);
         }
 #pragma unroll
-        for (int c = 0; c < 6; ++c) sg[c] = ld_stream(sig + c * nloc);
+        for (int c = 0; c < 6; ++c) sg[c] = ld_stream(sig + c * NP);
         if constexpr (NSLS > 0) {
             tau = ld_stream(a.tau + li);
 #pragma unroll
             for (int c = 0; c < 6; ++c)
 #pragma unroll
-                for (int q = 0; q < NSLS; ++q) m[c][q] = ld_stream(mem + (size_t)(c * NSLS + q) * nloc);
+                for (int q = 0; q < NSLS; ++q) m[c][q] = ld_stream(mem + (size_t)(c * NSLS + q) * NP);
         }
         T *my = sv + le * 3 * NP;
         my[p] = vx;
@@ -368,7 +370,7 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::M
     if (act) {
         const T *svx = sv + le * 3 * NP;
         point_step<N, T, NSLS, ANISO, DU>(a, sD, svx, svx + NP, svx + 2 * NP, p, i, j, k, ex, ey, ez, lam, mu, tau,
-                                          cA, cB, cC, sg, m, sig, mem, nloc, sf + le * 9 * NP,
+                                          cA, cB, cC, sg, m, sig, mem, NP, nloc, sf + le * 9 * NP,
                                           DU ? a.du + (size_t)s * 9 * nloc + li : nullptr);
     }
     __syncthreads();
@@ -460,13 +462,14 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT) k_element_pf(const StepArgs<T>
         if (le < EPB && e < a.nel) {
             const size_t li = (size_t)e * NP + p;
             T *st = stage + buf * NC * SLAB + o;
-            const T *sig = a.sig + (size_t)s * 6 * nloc + li;
+            const size_t sb = (size_t)e * S + s;
+            const T *sig = a.sig + sb * 6 * NP + p;
 #pragma unroll
-            for (int c = 0; c < 6; ++c) cp_async_stream(st + c * SLAB, sig + c * nloc, pol);
+            for (int c = 0; c < 6; ++c) cp_async_stream(st + c * SLAB, sig + c * NP, pol);
             if constexpr (NSLS > 0) {
-                const T *mem = a.mem + (size_t)s * 6 * NSLS * nloc + li;
+                const T *mem = a.mem + sb * 6 * NSLS * NP + p;
 #pragma unroll
-                for (int c = 0; c < 6 * NSLS; ++c) cp_async_stream(st + (6 + c) * SLAB, mem + c * nloc, pol);
+                for (int c = 0; c < 6 * NSLS; ++c) cp_async_stream(st + (6 + c) * SLAB, mem + c * NP, pol);
             }
             constexpr int b0 = 6 + 6 * NSLS;
             cp_async_stream(st + b0 * SLAB, a.lam + li, pol);
@@ -532,8 +535,9 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT) k_element_pf(const StepArgs<T>
             const size_t li = (size_t)e * NP + p;
             const T *svx = svb + b * 3 * SLAB + le * NP;
             point_step<N, T, NSLS, ANISO>(a, sD, svx, svx + SLAB, svx + 2 * SLAB, p, i, j, k, ex, ey, ez, lam, mu,
-                                          tau, cA, cB, cC, sg, m, a.sig + (size_t)s * 6 * nloc + li,
-                                          a.mem + (size_t)s * 6 * MS * nloc + li, nloc, sf + le * 9 * NP, nullptr);
+                                          tau, cA, cB, cC, sg, m, a.sig + ((size_t)e * S + s) * 6 * NP + p,
+                                          a.mem + ((size_t)e * S + s) * 6 * MS * NP + p, NP, nloc,
+                                          sf + le * 9 * NP, nullptr);
         }
         __syncthreads();  // fluxes complete; buffer b free for the group after next
         if (idx + 2 * stride < ngroups) prefetch(b, idx + 2 * stride);

@@ -53,6 +53,17 @@ namespace {
 thread_local std::string g_create_error;
 
 __global__ void k_set_it(int *d_it, int v) { *d_it = v; }
+
+// One component of the element-blocked stress / memory-variable state
+// [e][s][ncomp][NP] as an element-local field [e][NP] of simulation `sim`.
+template <typename T>
+__global__ void k_extract(const T *__restrict__ src, int S, int ncomp, int sim, int c, int NP, long long nel,
+                          T *__restrict__ out) {
+    const size_t li = (size_t)blockIdx.x * 256 + threadIdx.x;
+    if (li >= (size_t)nel * NP) return;
+    const size_t e = li / NP, p = li % NP;
+    out[li] = src[((e * S + sim) * ncomp + c) * NP + p];
+}
 __global__ void k_advance_it(int *d_it, int by) { *d_it += by; }
 
 // out[e*NP + p] = in[p*nel + e]: reference raw layout -> element-major, via
@@ -768,15 +779,19 @@ int field_source(sesnt_t *h, int sim, int which, T *scratch, const T **out, bool
     if (which >= 0 && which <= 2) {
         rc = o->gather_local(a, (const T *)h->v + ((size_t)sim * 3 + which) * nuni, scratch, h->stream);
     } else if (which >= 3 && which <= 8) {
-        *out = (const T *)h->sig + ((size_t)sim * 6 + (which - 3)) * nloc;
+        k_extract<T><<<(unsigned)((nloc + 255) / 256), 256, 0, h->stream>>>((const T *)h->sig, h->S, 6, sim,
+                                                                             which - 3, h->NP, h->nel, scratch);
+        rc = cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
     } else if (which == SESNT_FIELD_TAPER) {
         rc = o->taper_local(a, scratch, h->stream);
     } else if (which == SESNT_FIELD_MASS) {
         rc = o->gather_local(a, (const T *)h->invM, scratch, h->stream);
         *inverse = true;
     } else if (which >= SESNT_FIELD_MEMORY && which < SESNT_FIELD_MEMORY + 6 * kNsls && h->sls) {
-        const int c = (which - SESNT_FIELD_MEMORY) / kNsls, q = (which - SESNT_FIELD_MEMORY) % kNsls;
-        *out = (const T *)h->mem + ((size_t)sim * 6 * kNsls + c * kNsls + q) * nloc;
+        // memory variable (component c, mechanism q) at slot c*kNsls + q
+        k_extract<T><<<(unsigned)((nloc + 255) / 256), 256, 0, h->stream>>>(
+            (const T *)h->mem, h->S, 6 * kNsls, sim, which - SESNT_FIELD_MEMORY, h->NP, h->nel, scratch);
+        rc = cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
     } else if (which == SESNT_FIELD_PRESSURE) {
         rc = o->derived(a, which, sim, nullptr, scratch, h->stream);
     } else if (which >= SESNT_FIELD_EXX && which <= SESNT_FIELD_EZZ) {

@@ -209,8 +209,9 @@ __global__ void __launch_bounds__(TcCfg<N, PREC>::NT) k_element_tc(const StepArg
     size_t u = 0;
     T vx = 0, vy = 0, vz = 0, lam = 0, mu = 0, tau = 0, cA = 0, cB = 0, cC = 0;
     T sg[6] = {0, 0, 0, 0, 0, 0}, m[6][MS];
-    T *sig = a.sig + ((size_t)e * S + s) * 6 * NP + p;  // element-blocked [e][s][comp][p]
-    T *mem = a.mem + ((size_t)e * S + s) * 6 * MS * NP + p;
+    constexpr int NPS = state_stride(NP);  // element-blocked [e][s][comp][NPS]
+    T *sig = a.sig + ((size_t)e * S + s) * 6 * NPS + p;
+    T *mem = a.mem + ((size_t)e * S + s) * 6 * MS * NPS + p;
     if (act) {
         u = unique_index<N>(a.NXU, a.NYU, ex, ey, ez, i, j, k);
         const T *vs = a.v + (size_t)s * 3 * nuni;
@@ -225,13 +226,13 @@ __global__ void __launch_bounds__(TcCfg<N, PREC>::NT) k_element_tc(const StepArg
             cC = ld_stream(a.C + li);
         }
 #pragma unroll
-        for (int c = 0; c < 6; ++c) sg[c] = ld_stream(sig + c * NP);
+        for (int c = 0; c < 6; ++c) sg[c] = ld_stream(sig + c * NPS);
         if constexpr (NSLS > 0) {
             tau = ld_stream(a.tau + li);
 #pragma unroll
             for (int c = 0; c < 6; ++c)
 #pragma unroll
-                for (int q = 0; q < NSLS; ++q) m[c][q] = ld_stream(mem + (size_t)(c * NSLS + q) * NP);
+                for (int q = 0; q < NSLS; ++q) m[c][q] = ld_stream(mem + (size_t)(c * NSLS + q) * NPS);
         }
         // velocity into the gradient operand: x rows (j,k), y rows (i,k), z rows (i,j)
         const T vv[3] = {vx, vy, vz};
@@ -259,7 +260,7 @@ __global__ void __launch_bounds__(TcCfg<N, PREC>::NT) k_element_tc(const StepArg
 #pragma unroll
         for (int q = 0; q < 9; ++q) ev[q] = slab[q * NP + p];
         point_update<N, T, NSLS, ANISO>(a, ev, vx, vy, vz, p, i, j, k, ex, ey, ez, lam, mu, tau, cA, cB, cC, sg, m,
-                                        sig, mem, NP, nloc, slab, nullptr);
+                                        sig, mem, NPS, nloc, slab, nullptr);
         // fluxes slab[(c*3 + d)*NP + p] (force component c, direction d) into the divergence operand
 #pragma unroll
         for (int c = 0; c < 3; ++c) {

@@ -334,10 +334,11 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::M
     T lam = 0, mu = 0, tau = 0, cA = 0, cB = 0, cC = 0;
     T sg[6] = {0, 0, 0, 0, 0, 0};
     T m[6][MS];
-    // stress and memory variables: element-blocked [e][s][comp][p]
+    // stress and memory variables: element-blocked [e][s][comp][NPS]
+    constexpr int NPS = state_stride(NP);
     const size_t sb = (size_t)e * S + s;
-    T *sig = a.sig + sb * 6 * NP + p;
-    T *mem = a.mem + sb * 6 * MS * NP + p;
+    T *sig = a.sig + sb * 6 * NPS + p;
+    T *mem = a.mem + sb * 6 * MS * NPS + p;
     if (act) {
         ex = e % a.nx;
         ey = (e / a.nx) % a.ny;
@@ -353,13 +354,13 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::M
             cC = ld_stream(a.C + li);
         }
 #pragma unroll
-        for (int c = 0; c < 6; ++c) sg[c] = ld_stream(sig + c * NP);
+        for (int c = 0; c < 6; ++c) sg[c] = ld_stream(sig + c * NPS);
         if constexpr (NSLS > 0) {
             tau = ld_stream(a.tau + li);
 #pragma unroll
             for (int c = 0; c < 6; ++c)
 #pragma unroll
-                for (int q = 0; q < NSLS; ++q) m[c][q] = ld_stream(mem + (size_t)(c * NSLS + q) * NP);
+                for (int q = 0; q < NSLS; ++q) m[c][q] = ld_stream(mem + (size_t)(c * NSLS + q) * NPS);
         }
         T *my = sv + le * 3 * NP;
         my[p] = vx;
@@ -370,7 +371,7 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::M
     if (act) {
         const T *svx = sv + le * 3 * NP;
         point_step<N, T, NSLS, ANISO, DU>(a, sD, svx, svx + NP, svx + 2 * NP, p, i, j, k, ex, ey, ez, lam, mu, tau,
-                                          cA, cB, cC, sg, m, sig, mem, NP, nloc, sf + le * 9 * NP,
+                                          cA, cB, cC, sg, m, sig, mem, NPS, nloc, sf + le * 9 * NP,
                                           DU ? a.du + (size_t)s * 9 * nloc + li : nullptr);
     }
     __syncthreads();
@@ -462,14 +463,15 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT) k_element_pf(const StepArgs<T>
         if (le < EPB && e < a.nel) {
             const size_t li = (size_t)e * NP + p;
             T *st = stage + buf * NC * SLAB + o;
+            constexpr int NPS = state_stride(NP);
             const size_t sb = (size_t)e * S + s;
-            const T *sig = a.sig + sb * 6 * NP + p;
+            const T *sig = a.sig + sb * 6 * NPS + p;
 #pragma unroll
-            for (int c = 0; c < 6; ++c) cp_async_stream(st + c * SLAB, sig + c * NP, pol);
+            for (int c = 0; c < 6; ++c) cp_async_stream(st + c * SLAB, sig + c * NPS, pol);
             if constexpr (NSLS > 0) {
-                const T *mem = a.mem + sb * 6 * NSLS * NP + p;
+                const T *mem = a.mem + sb * 6 * NSLS * NPS + p;
 #pragma unroll
-                for (int c = 0; c < 6 * NSLS; ++c) cp_async_stream(st + (6 + c) * SLAB, mem + c * NP, pol);
+                for (int c = 0; c < 6 * NSLS; ++c) cp_async_stream(st + (6 + c) * SLAB, mem + c * NPS, pol);
             }
             constexpr int b0 = 6 + 6 * NSLS;
             cp_async_stream(st + b0 * SLAB, a.lam + li, pol);
@@ -532,11 +534,11 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT) k_element_pf(const StepArgs<T>
                 cB = st[(b1 + 1) * SLAB];
                 cC = st[(b1 + 2) * SLAB];
             }
-            const size_t li = (size_t)e * NP + p;
+            constexpr int NPS = state_stride(NP);
             const T *svx = svb + b * 3 * SLAB + le * NP;
             point_step<N, T, NSLS, ANISO>(a, sD, svx, svx + SLAB, svx + 2 * SLAB, p, i, j, k, ex, ey, ez, lam, mu,
-                                          tau, cA, cB, cC, sg, m, a.sig + ((size_t)e * S + s) * 6 * NP + p,
-                                          a.mem + ((size_t)e * S + s) * 6 * MS * NP + p, NP, nloc,
+                                          tau, cA, cB, cC, sg, m, a.sig + ((size_t)e * S + s) * 6 * NPS + p,
+                                          a.mem + ((size_t)e * S + s) * 6 * MS * NPS + p, NPS, nloc,
                                           sf + le * 9 * NP, nullptr);
         }
         __syncthreads();  // fluxes complete; buffer b free for the group after next

@@ -62,7 +62,7 @@ __global__ void k_extract(const T *__restrict__ src, int S, int ncomp, int sim, 
     const size_t li = (size_t)blockIdx.x * 256 + threadIdx.x;
     if (li >= (size_t)nel * NP) return;
     const size_t e = li / NP, p = li % NP;
-    out[li] = src[((e * S + sim) * ncomp + c) * NP + p];
+    out[li] = src[((e * S + sim) * ncomp + c) * (size_t)state_stride(NP) + p];
 }
 __global__ void k_advance_it(int *d_it, int by) { *d_it += by; }
 
@@ -446,8 +446,8 @@ const LpdOps<T> *ops(const sesnt_t *h) {
 int zero_state(sesnt_t *h) {
     const size_t E = h->esize;
     struct Z { void *p; size_t n; } zs[] = {
-        {h->sig, E * 6 * (size_t)h->nloc * h->S},
-        {h->mem, h->sls ? E * 6 * kNsls * (size_t)h->nloc * h->S : 0},
+        {h->sig, E * 6 * (size_t)h->nel * state_stride(h->NP) * h->S},
+        {h->mem, h->sls ? E * 6 * kNsls * (size_t)h->nel * state_stride(h->NP) * h->S : 0},
         {h->v, E * 3 * (size_t)h->nuni * h->S},
         {h->vc, h->kahan ? E * 3 * (size_t)h->nuni * h->S : 0},
         {h->F, E * 3 * (size_t)h->nuni * h->S},
@@ -1069,7 +1069,7 @@ size_t footprint(const sesnt_grid_t *g, bool aniso) {
     const size_t E = g->precision == 8 ? 8 : 4, S = g->batch;
     size_t b = 0;
     b += nloc * E * (2 + (aniso ? 3 : 0) + (g->n_sls ? 1 : 0));    // lambda, mu, A,B,C, tau
-    b += nloc * E * S * (6 + (g->n_sls ? 6 * kNsls : 0));          // sigma, memory
+    b += nel * state_stride((int)NP) * E * S * (6 + (g->n_sls ? 6 * kNsls : 0));  // sigma, memory
     b += nuni * E * (1 + S * (6 + ((g->flags & SESNT_FLAG_KAHAN) ? 3 : 0)));  // invM, v, F, comp
     b += nloc * E * S * (((g->flags & SESNT_FLAG_STRAIN) ? 9 : 0) + ((g->flags & SESNT_FLAG_ROTATION) ? 6 : 0));
     b += nloc * (sizeof(float) + E);                                // set_model staging + rhoinv (transient)
@@ -1137,7 +1137,7 @@ int sesnt_create(const sesnt_grid_t *grid, sesnt_t **out) {
         {(void **)&h->dsin, grid->nx * P * 8, "dsin"}, {(void **)&h->dr, grid->nz * P * 8, "dr"},
         {(void **)&h->dw, P * 8, "dw"},
         {&h->lam, nloc * E, "lambda"}, {&h->mu, nloc * E, "mu"},
-        {&h->sig, 6 * nloc * E * S, "stress"},
+        {&h->sig, 6 * (size_t)h->nel * state_stride(h->NP) * E * S, "stress"},
         {&h->v, 3 * nuni * E * S, "velocity"}, {&h->F, 3 * nuni * E * S, "force"},
         {&h->invM, nuni * E, "inverse mass"}, {(void **)&h->d_it, sizeof(int), "step counter"},
         {(void **)&h->d_err, sizeof(int), "error word"}};
@@ -1147,7 +1147,7 @@ int sesnt_create(const sesnt_grid_t *grid, sesnt_t **out) {
             return rc;
         }
     if (h->sls) {
-        if ((rc = h->alloc(&h->tau, nloc * E, "tau")) || (rc = h->alloc(&h->mem, 6 * kNsls * nloc * E * S, "memory"))) {
+        if ((rc = h->alloc(&h->tau, nloc * E, "tau")) || (rc = h->alloc(&h->mem, 6 * kNsls * (size_t)h->nel * state_stride(h->NP) * E * S, "memory"))) {
             g_create_error = h->err;
             return rc;
         }

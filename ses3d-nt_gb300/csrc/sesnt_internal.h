@@ -96,6 +96,16 @@ struct StepArgs {
     int nxtr, nrot;
 };
 
+// Points per element in the element-blocked stress / memory-variable state
+// [e][s][comp][NPS]: NP padded to a multiple of 4 so that every chunk starts
+// on a 16-byte boundary (coalesced warps, bulk-copy alignment).
+#ifdef __CUDACC__
+#define SESNT_HD __host__ __device__
+#else
+#define SESNT_HD
+#endif
+SESNT_HD constexpr int state_stride(int np) { return (np + 3) & ~3; }
+
 // Displacement-gradient components (src/evolution.f90:179-187).
 enum { kDuXX = 0, kDuYY, kDuZZ, kDuXY, kDuYX, kDuXZ, kDuZX, kDuYZ, kDuZY };
 // Rotation strain: the gradient components the reference's rot_v channels

@@ -51,8 +51,9 @@ extern "C" {
 #define SESNT_FLAG_TC_TF32X3 8u   /* derivative and divergence contractions on the tensor cores
                                      (tcgen05) in split TF32 (3 products), FP32 accumulation */
 #define SESNT_FLAG_TC_BF16X3 16u  /* the same in split BF16 (3 products); FP32 wavefields only */
-#define SESNT_FLAG_PERSISTENT_ELEMENT 4u /* persistent element kernel that prefetches the next
-                                            element groups with cp.async (same results) */
+#define SESNT_FLAG_PERSISTENT_ELEMENT 4u /* persistent element kernel fed by bulk copies (TMA):
+                                            each element's stress and memory variables move as
+                                            whole chunks, loaded a few elements ahead (same results) */
 #define SESNT_FLAG_STRAIN 32u     /* keep the displacement gradient (src/evolution.f90:179-187):
                                      9 more element-local fields read and written each step;
                                      enables SESNT_FIELD_EXX .. _EZZ */
@@ -225,7 +226,8 @@ int sesnt_synchronize(sesnt_t *h);
 int sesnt_reset(sesnt_t *h);
 
 /* No counterpart in the reference. Failure-detection hook: every device-side
- * completion wait (the tensor-core element kernel's mbarrier waits) gives up
+ * completion wait (the mbarrier waits of the tensor-core and of the
+ * bulk-copy element kernels) gives up
  * after `polls` polls (default 4,194,304), sets the handle's error word and
  * leaves the state of its points unchanged; the next synchronising call then
  * returns SESNT_ETIMEOUT until sesnt_reset. drop_completion != 0 makes that

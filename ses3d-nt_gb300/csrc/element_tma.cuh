@@ -1,0 +1,269 @@
+// Persistent element kernel fed by the tensor memory accelerator (bulk
+// copies). Each element's stress and memory variables are one contiguous,
+// 16-byte aligned chunk of the element-blocked state ([e][s][comp][NPS]), so
+// one cp.async.bulk per array moves a whole element into shared memory,
+// tracked by an mbarrier with a transaction count, NSTAGE-1 elements ahead of
+// the one being computed. The updated state is written back into the same
+// shared-memory stage and stored with one bulk copy per array
+// (cp.async.bulk ... bulk_group), so the streaming traffic costs no per-thread
+// load/store instructions and no registers. Velocity gathers, material and
+// the contractions are as in k_element.
+//
+// Per block (one element at a time, thread p owns point p):
+//   wait stage k%NSTAGE -> velocity slab -> point update (state read from and
+//   written to the stage) -> bulk store of the stage -> bulk load of element
+//   k+NSTAGE-1 into the stage element k-1 used (after its store has read it)
+//   -> weak divergence and atomic assembly.
+// Every mbarrier wait is bounded (StepArgs::wait_polls); on expiry the block
+// sets the error word and leaves the loop with all its threads.
+#pragma once
+
+namespace sesnt {
+
+__device__ __forceinline__ uint32_t tma_smem(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void tma_mbar_init(uint32_t mbar) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(mbar) : "memory");
+}
+
+// Arrive once and add `bytes` to the transaction count of this phase.
+__device__ __forceinline__ void tma_expect(uint32_t mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(mbar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void tma_load(uint32_t dst, const void *src, uint32_t bytes, uint32_t mbar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(mbar)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tma_store(void *dst, uint32_t src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(src), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void tma_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+
+// Wait until at most NPEND committed bulk groups of this thread still read
+// shared memory (their source may then be overwritten).
+template <int NPEND>
+__device__ __forceinline__ void tma_wait_read() {
+    asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(NPEND) : "memory");
+}
+
+// Wait until every committed bulk group of this thread has completed.
+__device__ __forceinline__ void tma_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+__device__ __forceinline__ bool tma_try_wait(uint32_t mbar, uint32_t parity, int polls) {
+    uint32_t done = 0;
+    for (int it = 0; it < polls && !done; ++it)
+        asm volatile(
+            "{.reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p;}"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+    return done != 0;
+}
+
+// Stages of the bulk-copy pipeline: loads run NSTAGE-1 elements ahead.
+#ifndef SESNT_TMA_STAGES
+#define SESNT_TMA_STAGES 3
+#endif
+
+template <int N, typename T, int NSLS>
+struct TmaCfg {
+    static constexpr int P = N + 1, NP = P * P * P, NPS = state_stride(NP);
+    static constexpr int NT = ((NP + 31) / 32) * 32;
+    static constexpr int MS = NSLS > 0 ? NSLS : 1;
+    static constexpr int NSTAGE = SESNT_TMA_STAGES;
+    static constexpr uint32_t SIG_BYTES = 6 * NPS * sizeof(T);
+    static constexpr uint32_t MEM_BYTES = NSLS > 0 ? 6 * NSLS * NPS * sizeof(T) : 0;
+    static constexpr uint32_t STAGE_BYTES = SIG_BYTES + MEM_BYTES;  // a multiple of 16
+    // stages, then sD [4][P*P], sv [3][NP], sf [9][NP], then the mbarriers
+    static constexpr size_t SMALL = sizeof(T) * (4 * P * P + 12 * NP);
+    static constexpr size_t SMEM = NSTAGE * (size_t)STAGE_BYTES + ((SMALL + 15) / 16) * 16 + 8 * NSTAGE;
+    // resident blocks the register allocation is sized for: as many as the
+    // shared memory allows, at most 8 and at most 2048 threads
+    static constexpr int MINB_RAW = (int)((227 * 1024) / SMEM);
+    static constexpr int MINB_CAP = (2048 / NT) < 8 ? (2048 / NT) : 8;
+    static constexpr int MINB = MINB_RAW < 1 ? 1 : (MINB_RAW > MINB_CAP ? MINB_CAP : MINB_RAW);
+};
+
+template <int N, typename T, int NSLS, bool ANISO>
+__global__ void __launch_bounds__(TmaCfg<N, T, NSLS>::NT, TmaCfg<N, T, NSLS>::MINB) k_element_tma(const StepArgs<T> a) {
+    using C = TmaCfg<N, T, NSLS>;
+    constexpr int P = C::P, NP = C::NP, NPS = C::NPS, NT = C::NT, MS = C::MS, NSTAGE = C::NSTAGE;
+    extern __shared__ __align__(128) unsigned char tma_smem_raw[];
+    unsigned char *stage0 = tma_smem_raw;
+    T *sD = reinterpret_cast<T *>(tma_smem_raw + NSTAGE * (size_t)C::STAGE_BYTES);
+    T *sv = sD + 4 * P * P;
+    T *sf = sv + 3 * NP;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(tma_smem_raw + NSTAGE * (size_t)C::STAGE_BYTES +
+                                                  ((C::SMALL + 15) / 16) * 16);
+
+    const int t = threadIdx.x;
+    const int S = a.S;
+    const long long units = (long long)a.nel * S;
+    const long long first = blockIdx.x, stride = gridDim.x;
+    const int count = first < units ? (int)((units - 1 - first) / stride + 1) : 0;
+    if (count == 0) return;
+    const size_t nuni = (size_t)a.nuni, nloc = (size_t)a.nloc;
+
+    for (int x = t; x < 4 * P * P; x += NT) sD[x] = a.tabD[x];
+    if (t == 0) {
+        for (int b = 0; b < NSTAGE; ++b) tma_mbar_init(tma_smem(mbar + b));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    // bulk loads of unit k (this block's k-th element-simulation) into stage k % NSTAGE
+    auto issue_load = [&](int k) {
+        if (a.drop_completion) return;  // failure-detection test: the stage never lands
+        const long long g = first + (long long)k * stride;
+        const int b = k % NSTAGE;
+        unsigned char *st = stage0 + (size_t)b * C::STAGE_BYTES;
+        const uint32_t mb = tma_smem(mbar + b);
+        tma_expect(mb, C::STAGE_BYTES);
+        tma_load(tma_smem(st), a.sig + (size_t)g * 6 * NPS, C::SIG_BYTES, mb);
+        if constexpr (NSLS > 0) tma_load(tma_smem(st + C::SIG_BYTES), a.mem + (size_t)g * 6 * NSLS * NPS, C::MEM_BYTES, mb);
+    };
+    if (t == 0)
+        for (int k = 0; k < NSTAGE - 1 && k < count; ++k) issue_load(k);
+
+    const int p = t;
+    const bool act = p < NP;
+    const int i = p % P, j = (p / P) % P, k3 = p / (P * P);
+    // velocity and material of unit k, gathered ahead into registers
+    T nv[3] = {0, 0, 0}, nlam = 0, nmu = 0, ntau = 0, nA = 0, nB = 0, nC = 0;
+    auto gather = [&](int k) {
+        if (!act || k >= count) return;
+        const long long g = first + (long long)k * stride;
+        const int e = (int)(g / S), s = (int)(g % S);
+        const int ex = e % a.nx, ey = (e / a.nx) % a.ny, ez = e / (a.nx * a.ny);
+        const size_t u = unique_index<N>(a.NXU, a.NYU, ex, ey, ez, i, j, k3);
+        const T *vs = a.v + (size_t)s * 3 * nuni;
+        nv[0] = vs[u];
+        nv[1] = vs[nuni + u];
+        nv[2] = vs[2 * nuni + u];
+        const size_t li = (size_t)e * NP + p;
+        nlam = a.lam[li];
+        nmu = a.mu[li];
+        if constexpr (NSLS > 0) ntau = a.tau[li];
+        if constexpr (ANISO) {
+            nA = a.A[li];
+            nB = a.B[li];
+            nC = a.C[li];
+        }
+    };
+    gather(0);
+
+    bool ok = true;
+    int kfail = count;
+    for (int k = 0; k < count; ++k) {
+        const long long g = first + (long long)k * stride;
+        const int e = (int)(g / S), s = (int)(g % S);
+        const int ex = e % a.nx, ey = (e / a.nx) % a.ny, ez = e / (a.nx * a.ny);
+        const int b = k % NSTAGE;
+        T *st = reinterpret_cast<T *>(stage0 + (size_t)b * C::STAGE_BYTES);
+        const T vx = nv[0], vy = nv[1], vz = nv[2], lam = nlam, mu = nmu, tau = ntau, cA = nA, cB = nB, cC = nC;
+        if (act) {
+            sv[p] = vx;
+            sv[NP + p] = vy;
+            sv[2 * NP + p] = vz;
+        }
+        // the stage of unit k has landed (block-uniform outcome)
+        ok = __syncthreads_and(tma_try_wait(tma_smem(mbar + b), (uint32_t)((k / NSTAGE) & 1), a.wait_polls)) != 0;
+        if (!ok) {
+            kfail = k;
+            break;
+        }
+        gather(k + 1);  // next unit's velocity and material, in flight during this one
+        size_t u = 0;
+        if (act) {
+            u = unique_index<N>(a.NXU, a.NYU, ex, ey, ez, i, j, k3);
+            T sg[6], m[6][MS];
+#pragma unroll
+            for (int c = 0; c < 6; ++c) sg[c] = st[c * NPS + p];
+            if constexpr (NSLS > 0) {
+#pragma unroll
+                for (int c = 0; c < 6; ++c)
+#pragma unroll
+                    for (int q = 0; q < NSLS; ++q) m[c][q] = st[(6 + c * NSLS + q) * NPS + p];
+            }
+            T ev[9];
+            strain_contract<N, T>(sD, sv, sv + NP, sv + 2 * NP, i, j, k3, ev);
+            point_update<N, T, NSLS, ANISO, false, true>(a, ev, vx, vy, vz, p, i, j, k3, ex, ey, ez, lam, mu, tau,
+                                                         cA, cB, cC, sg, m, st + p, st + 6 * NPS + p, NPS, nloc, sf,
+                                                         nullptr);
+        }
+        // state written back into the stage: hand it to the bulk-copy engine
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (t == 0) {
+            tma_store(a.sig + (size_t)g * 6 * NPS, tma_smem(st), C::SIG_BYTES);
+            if constexpr (NSLS > 0)
+                tma_store(a.mem + (size_t)g * 6 * NSLS * NPS, tma_smem(reinterpret_cast<unsigned char *>(st) + C::SIG_BYTES),
+                          C::MEM_BYTES);
+            tma_commit();
+            if (k + NSTAGE - 1 < count) {
+                // stage (k-1) % NSTAGE: its store (the group before this one) must have read it
+                tma_wait_read<1>();
+                issue_load(k + NSTAGE - 1);
+            }
+        }
+        if (act) {
+            T fx = 0, fy = 0, fz = 0;
+            point_divergence<N, T>(sD + 3 * P * P, sf, i, j, k3, fx, fy, fz);
+            T *F = a.F + (size_t)s * 3 * nuni;
+            atomicAdd(F + u, fx);
+            atomicAdd(F + nuni + u, fy);
+            atomicAdd(F + 2 * nuni + u, fz);
+        }
+        __syncthreads();  // sv and sf are rewritten by the next unit
+    }
+    if (!ok && t == 0) atomicExch(a.err, 1);
+    if (t == 0) tma_wait_all();  // stores complete; loads of a failed run are waited for below
+    if (!ok) {
+        // the loads issued for units kfail .. kfail+NSTAGE-2 may still be in
+        // flight: one more bounded wait each before the shared memory is released
+        for (int k = kfail; k < count && k < kfail + NSTAGE - 1; ++k)
+            tma_try_wait(tma_smem(mbar + (k % NSTAGE)), (uint32_t)((k / NSTAGE) & 1), a.wait_polls);
+    }
+}
+
+// Resident blocks per SM of the TMA kernel (filled in by prepare, outside capture).
+template <int N, typename T, int NSLS, bool ANISO>
+struct TmaLaunch {
+    static int blocks;
+};
+template <int N, typename T, int NSLS, bool ANISO>
+int TmaLaunch<N, T, NSLS, ANISO>::blocks = 0;
+
+template <int N, typename T, int NSLS, bool ANISO>
+int prepare_element_tma() {
+    using C = TmaCfg<N, T, NSLS>;
+    if (C::SMEM > kMaxSmemPerBlock) return 0;
+    cudaError_t e = cudaFuncSetAttribute(k_element_tma<N, T, NSLS, ANISO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)C::SMEM);
+    int dev = 0, nb = 0, sms = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_element_tma<N, T, NSLS, ANISO>, C::NT, C::SMEM);
+    if (e == cudaSuccess) TmaLaunch<N, T, NSLS, ANISO>::blocks = nb * sms;
+    return e == cudaSuccess ? 0 : -1;
+}
+
+// Launches the TMA kernel; returns 1 if this configuration has none (the
+// caller then falls back to the one-block-per-group kernel).
+template <int N, typename T, int NSLS, bool ANISO>
+int launch_element_tma(const StepArgs<T> &a, void *stream) {
+    using C = TmaCfg<N, T, NSLS>;
+    const int resident = TmaLaunch<N, T, NSLS, ANISO>::blocks;
+    if (C::SMEM > kMaxSmemPerBlock || resident <= 0) return 1;
+    const long long units = (long long)a.nel * a.S;
+    const long long blocks = std::min<long long>(units, resident);
+    k_element_tma<N, T, NSLS, ANISO><<<(unsigned)blocks, C::NT, C::SMEM, (cudaStream_t)stream>>>(a);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace sesnt

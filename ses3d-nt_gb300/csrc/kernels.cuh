@@ -22,6 +22,9 @@
 //              (:393-402), force reset for the next step.
 //   k_receivers one warp per receiver: Lagrange interpolation of v
 //              (channel_mod.f90:505-592).
+// Variants of the element kernel: element_tc.cuh (tcgen05 contractions),
+// element_tma.cuh (persistent, state moved by bulk copies); channels.cuh holds
+// the receiver-channel and snapshot-field kernels.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -163,8 +166,9 @@ __device__ __forceinline__ void complete_gradient(const StepArgs<T> &a, const T 
 // The rest of one element-local point's step, from its raw velocity gradient
 // e[9] (layout of strain_contract) and velocity. DU: integrate this point's
 // displacement gradient `du` (stride nloc); a compile-time switch, since even
-// a skipped branch measured 1.5% on the step.
-template <int N, typename T, int NSLS, bool ANISO, bool DU = false>
+// a skipped branch measured 1.5% on the step. SMEM: sig/mem point into shared
+// memory (plain stores instead of streaming global stores).
+template <int N, typename T, int NSLS, bool ANISO, bool DU = false, bool SMEM = false>
 __device__ __forceinline__ void point_update(const StepArgs<T> &a, const T (&e)[9], T vx, T vy, T vz, int p, int i,
                                              int j, int k, int ex, int ey, int ez, T lam, T mu, T tau, T cA, T cB,
                                              T cC, const T (&sg)[6], const T (&m)[6][NSLS > 0 ? NSLS : 1], T *sig,
@@ -234,12 +238,16 @@ __device__ __forceinline__ void point_update(const StepArgs<T> &a, const T (&e)[
     const T syz = sg[4] + a.dt * ryz;
     const T szz = sg[5] + a.dt * rzz;
     const T tp = taper_value(a.px[ex * P + i], a.py[ey * P + j], a.pz[ez * P + k], a.inv_alpha);
-    st_stream(sig, sxx * tp);
-    st_stream(sig + cs, sxy * tp);
-    st_stream(sig + 2 * cs, sxz * tp);
-    st_stream(sig + 3 * cs, syy * tp);
-    st_stream(sig + 4 * cs, syz * tp);
-    st_stream(sig + 5 * cs, szz * tp);
+    auto put = [](T *q, T v) {
+        if constexpr (SMEM) *q = v;
+        else st_stream(q, v);
+    };
+    put(sig, sxx * tp);
+    put(sig + cs, sxy * tp);
+    put(sig + 2 * cs, sxz * tp);
+    put(sig + 3 * cs, syy * tp);
+    put(sig + 4 * cs, syz * tp);
+    put(sig + 5 * cs, szz * tp);
     if constexpr (NSLS > 0) {
         // memory variables after the update, driven by this step's rates:
         // M <- M*(1 - dt/tau_p) - tau*dt/(n*tau_p)*e
@@ -249,7 +257,7 @@ __device__ __forceinline__ void point_update(const StepArgs<T> &a, const T (&e)[
             const T drive = tau * a.mem_drive[q];
 #pragma unroll
             for (int c = 0; c < 6; ++c)
-                st_stream(mem + (size_t)(c * NSLS + q) * cs, m[c][q] * a.mem_keep[q] - drive * er[c]);
+                put(mem + (size_t)(c * NSLS + q) * cs, m[c][q] * a.mem_keep[q] - drive * er[c]);
         }
     }
     // metric-weighted stresses for the weak divergence
@@ -385,176 +393,6 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::M
     }
 }
 
-// ---------------------------------------------------------------------------
-// Persistent variant: each block walks element groups (g, s) with a stride of
-// the grid and stages the next groups' streamed data (stress, memory
-// variables, material) and velocity gather in shared memory with cp.async
-// while it computes the current one (double buffer), so every SM keeps loads
-// in flight through the compute and store phases.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ unsigned long long evict_first_policy() {
-    unsigned long long pol;
-    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
-    return pol;
-}
-
-template <typename T>
-__device__ __forceinline__ void cp_async_stream(T *smem, const T *gmem, unsigned long long pol) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    if constexpr (sizeof(T) == 4)
-        asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 4, %2;" ::"r"(s), "l"(gmem), "l"(pol)
-                     : "memory");
-    else
-        asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 8, %2;" ::"r"(s), "l"(gmem), "l"(pol)
-                     : "memory");
-}
-
-template <typename T>
-__device__ __forceinline__ void cp_async_keep(T *smem, const T *gmem) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    if constexpr (sizeof(T) == 4)
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
-    else
-        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(gmem) : "memory");
-}
-
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-
-template <int K>
-__device__ __forceinline__ void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;" ::"n"(K) : "memory");
-}
-
-template <int N, typename T, int NSLS, bool ANISO>
-struct PfCfg {
-    static constexpr int NP = ElemCfg<N>::NP, EPB = ElemCfg<N>::EPB;
-    // streamed components: 6 stress, 6*NSLS memory, lambda, mu, [tau], [A,B,C]
-    static constexpr int NC = 6 + 6 * NSLS + 2 + (NSLS > 0 ? 1 : 0) + (ANISO ? 3 : 0);
-    static constexpr int SLAB = EPB * NP;
-    static constexpr size_t SMEM =
-        sizeof(T) * (4 * ElemCfg<N>::P * ElemCfg<N>::P + 2 * NC * SLAB + 2 * 3 * SLAB + 9 * SLAB);
-};
-
-template <int N, typename T, int NSLS, bool ANISO>
-__global__ void __launch_bounds__(ElemCfg<N>::NT) k_element_pf(const StepArgs<T> a) {
-    using C = PfCfg<N, T, NSLS, ANISO>;
-    constexpr int P = ElemCfg<N>::P, NP = ElemCfg<N>::NP, EPB = ElemCfg<N>::EPB, NT = ElemCfg<N>::NT;
-    constexpr int MS = NSLS > 0 ? NSLS : 1, NC = C::NC, SLAB = C::SLAB;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T *sD = reinterpret_cast<T *>(smem_raw);  // [4][P*P]
-    T *stage = sD + 4 * P * P;                // [2][NC][SLAB]
-    T *svb = stage + 2 * NC * SLAB;           // [2][3][SLAB]
-    T *sf = svb + 2 * 3 * SLAB;               // [9][SLAB] (element le at offset le*9*NP)
-
-    const int t = threadIdx.x;
-    for (int x = t; x < 4 * P * P; x += NT) sD[x] = a.tabD[x];
-    const int le = t / NP;
-    const int p = t - le * NP;
-    const int i = p % P, j = (p / P) % P, k = p / (P * P);
-    const int o = le * NP + p;  // this thread's slot in a slab
-    const size_t nuni = (size_t)a.nuni, nloc = (size_t)a.nloc;
-    const int S = a.S;
-    const long long ngroups = (long long)((a.nel + EPB - 1) / EPB) * S;
-    const unsigned long long pol = evict_first_policy();
-
-    auto prefetch = [&](int buf, long long idx) {
-        const int s = (int)(idx % S);
-        const int e = (int)(idx / S) * EPB + le;
-        if (le < EPB && e < a.nel) {
-            const size_t li = (size_t)e * NP + p;
-            T *st = stage + buf * NC * SLAB + o;
-            constexpr int NPS = state_stride(NP);
-            const size_t sb = (size_t)e * S + s;
-            const T *sig = a.sig + sb * 6 * NPS + p;
-#pragma unroll
-            for (int c = 0; c < 6; ++c) cp_async_stream(st + c * SLAB, sig + c * NPS, pol);
-            if constexpr (NSLS > 0) {
-                const T *mem = a.mem + sb * 6 * NSLS * NPS + p;
-#pragma unroll
-                for (int c = 0; c < 6 * NSLS; ++c) cp_async_stream(st + (6 + c) * SLAB, mem + c * NPS, pol);
-            }
-            constexpr int b0 = 6 + 6 * NSLS;
-            cp_async_stream(st + b0 * SLAB, a.lam + li, pol);
-            cp_async_stream(st + (b0 + 1) * SLAB, a.mu + li, pol);
-            if constexpr (NSLS > 0) cp_async_stream(st + (b0 + 2) * SLAB, a.tau + li, pol);
-            if constexpr (ANISO) {
-                constexpr int b1 = b0 + 2 + (NSLS > 0 ? 1 : 0);
-                cp_async_stream(st + b1 * SLAB, a.A + li, pol);
-                cp_async_stream(st + (b1 + 1) * SLAB, a.B + li, pol);
-                cp_async_stream(st + (b1 + 2) * SLAB, a.C + li, pol);
-            }
-            const int ex = e % a.nx, ey = (e / a.nx) % a.ny, ez = e / (a.nx * a.ny);
-            const size_t u = unique_index<N>(a.NXU, a.NYU, ex, ey, ez, i, j, k);
-            const T *vs = a.v + (size_t)s * 3 * nuni + u;
-            T *sv = svb + buf * 3 * SLAB + o;
-            cp_async_keep(sv, vs);
-            cp_async_keep(sv + SLAB, vs + nuni);
-            cp_async_keep(sv + 2 * SLAB, vs + 2 * nuni);
-        }
-        cp_async_commit();
-    };
-
-    long long idx = blockIdx.x;
-    const long long stride = gridDim.x;
-    if (idx < ngroups) prefetch(0, idx);
-    else cp_async_commit();
-    if (idx + stride < ngroups) prefetch(1, idx + stride);
-    else cp_async_commit();
-    for (int it = 0; idx < ngroups; idx += stride, ++it) {
-        const int b = it & 1;
-        const int s = (int)(idx % S);
-        const int e = (int)(idx / S) * EPB + le;
-        const bool act = (le < EPB) && (e < a.nel);
-        cp_async_wait<1>();  // this group's copies have landed (the next group's may still fly)
-        __syncthreads();     // ... and are visible to the whole block
-        int ex = 0, ey = 0, ez = 0;
-        size_t u = 0;
-        if (act) {
-            ex = e % a.nx;
-            ey = (e / a.nx) % a.ny;
-            ez = e / (a.nx * a.ny);
-            u = unique_index<N>(a.NXU, a.NYU, ex, ey, ez, i, j, k);
-            const T *st = stage + b * NC * SLAB + o;
-            T sg[6], m[6][MS];
-#pragma unroll
-            for (int c = 0; c < 6; ++c) sg[c] = st[c * SLAB];
-            if constexpr (NSLS > 0) {
-#pragma unroll
-                for (int c = 0; c < 6; ++c)
-#pragma unroll
-                    for (int q = 0; q < NSLS; ++q) m[c][q] = st[(6 + c * NSLS + q) * SLAB];
-            }
-            constexpr int b0 = 6 + 6 * NSLS;
-            const T lam = st[b0 * SLAB], mu = st[(b0 + 1) * SLAB];
-            T tau = 0, cA = 0, cB = 0, cC = 0;
-            if constexpr (NSLS > 0) tau = st[(b0 + 2) * SLAB];
-            if constexpr (ANISO) {
-                constexpr int b1 = b0 + 2 + (NSLS > 0 ? 1 : 0);
-                cA = st[b1 * SLAB];
-                cB = st[(b1 + 1) * SLAB];
-                cC = st[(b1 + 2) * SLAB];
-            }
-            constexpr int NPS = state_stride(NP);
-            const T *svx = svb + b * 3 * SLAB + le * NP;
-            point_step<N, T, NSLS, ANISO>(a, sD, svx, svx + SLAB, svx + 2 * SLAB, p, i, j, k, ex, ey, ez, lam, mu,
-                                          tau, cA, cB, cC, sg, m, a.sig + ((size_t)e * S + s) * 6 * NPS + p,
-                                          a.mem + ((size_t)e * S + s) * 6 * MS * NPS + p, NPS, nloc,
-                                          sf + le * 9 * NP, nullptr);
-        }
-        __syncthreads();  // fluxes complete; buffer b free for the group after next
-        if (idx + 2 * stride < ngroups) prefetch(b, idx + 2 * stride);
-        else cp_async_commit();
-        if (act) {
-            T fx = 0, fy = 0, fz = 0;
-            point_divergence<N, T>(sD + 3 * P * P, sf + le * 9 * NP, i, j, k, fx, fy, fz);
-            T *F = a.F + (size_t)s * 3 * nuni;
-            atomicAdd(F + u, fx);
-            atomicAdd(F + nuni + u, fy);
-            atomicAdd(F + 2 * nuni + u, fz);
-        }
-    }
-    cp_async_wait<0>();
-}
 
 // Source slabs through the weak divergence, one block per resolved
 // (simulation, element) record. The slab set after step it-1 acts in step it
@@ -812,40 +650,19 @@ __global__ void __launch_bounds__(256) k_taper_local(const StepArgs<T> a, T *loc
 // ---------------------------------------------------------------------------
 constexpr size_t kMaxSmemPerBlock = 227 * 1024;
 
-// Resident blocks per SM and SM count for the persistent variant, filled in
-// by prepare_element (outside stream capture).
-template <int N, typename T, int NSLS, bool ANISO>
-struct PfLaunch {
-    static int blocks_per_sm;
-    static int sms;
-};
-template <int N, typename T, int NSLS, bool ANISO>
-int PfLaunch<N, T, NSLS, ANISO>::blocks_per_sm = 0;
-template <int N, typename T, int NSLS, bool ANISO>
-int PfLaunch<N, T, NSLS, ANISO>::sms = 0;
-
 template <int N, typename T, int NSLS, bool ANISO>
 int launch_element_v(const StepArgs<T> &a, void *stream) {
     using C = ElemCfg<N>;
-    using PF = PfCfg<N, T, NSLS, ANISO>;
-    using L = PfLaunch<N, T, NSLS, ANISO>;
     const long long groups = (long long)((a.nel + C::EPB - 1) / C::EPB) * a.S;
-    if (a.persistent && PF::SMEM <= kMaxSmemPerBlock && L::blocks_per_sm > 0) {
-        const long long blocks = std::min<long long>(groups, (long long)L::blocks_per_sm * L::sms);
-        k_element_pf<N, T, NSLS, ANISO><<<(unsigned)blocks, C::NT, PF::SMEM, (cudaStream_t)stream>>>(a);
-    } else {
-        const size_t smem = sizeof(T) * (4 * C::P * C::P + C::EPB * 12 * C::NP);
-        if (a.du) k_element<N, T, NSLS, ANISO, true><<<(unsigned)groups, C::NT, smem, (cudaStream_t)stream>>>(a);
-        else k_element<N, T, NSLS, ANISO, false><<<(unsigned)groups, C::NT, smem, (cudaStream_t)stream>>>(a);
-    }
+    const size_t smem = sizeof(T) * (4 * C::P * C::P + C::EPB * 12 * C::NP);
+    if (a.du) k_element<N, T, NSLS, ANISO, true><<<(unsigned)groups, C::NT, smem, (cudaStream_t)stream>>>(a);
+    else k_element<N, T, NSLS, ANISO, false><<<(unsigned)groups, C::NT, smem, (cudaStream_t)stream>>>(a);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
 template <int N, typename T, int NSLS, bool ANISO>
 int prepare_variant() {
     using C = ElemCfg<N>;
-    using PF = PfCfg<N, T, NSLS, ANISO>;
-    using L = PfLaunch<N, T, NSLS, ANISO>;
     const size_t smem = sizeof(T) * (4 * C::P * C::P + C::EPB * 12 * C::NP);
     cudaError_t e = cudaSuccess;
     if (smem > 48 * 1024)
@@ -854,30 +671,18 @@ int prepare_variant() {
     if (e == cudaSuccess && smem > 48 * 1024)
         e = cudaFuncSetAttribute(k_element<N, T, NSLS, ANISO, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem);
-    if (e == cudaSuccess && PF::SMEM <= kMaxSmemPerBlock) {
-        e = cudaFuncSetAttribute(k_element_pf<N, T, NSLS, ANISO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)PF::SMEM);
-        int dev = 0, nb = 0, sms = 0;
-        if (e == cudaSuccess) e = cudaGetDevice(&dev);
-        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_element_pf<N, T, NSLS, ANISO>, C::NT, PF::SMEM);
-        if (e == cudaSuccess) {
-            L::blocks_per_sm = nb;
-            L::sms = sms;
-        }
-    }
     return e == cudaSuccess ? 0 : -1;
 }
 
-// Kernel attributes (large dynamic shared memory) and the persistent grid
-// size, once per handle, outside stream capture.
 }  // namespace sesnt
 
 #include "element_tc.cuh"
+#include "element_tma.cuh"
 
 namespace sesnt {
 
+// Kernel attributes (large dynamic shared memory) and the resident-block
+// counts of the persistent kernel, once per handle, outside stream capture.
 template <int N, typename T>
 int prepare_element() {
     if (prepare_variant<N, T, 0, false>() || prepare_variant<N, T, 0, true>() ||
@@ -885,14 +690,29 @@ int prepare_element() {
         return -1;
     if constexpr (std::is_same_v<T, float>)
         if (prepare_element_tc<N, 1>() || prepare_element_tc<N, 2>()) return -1;
+    if (prepare_element_tma<N, T, 0, false>() || prepare_element_tma<N, T, 0, true>() ||
+        prepare_element_tma<N, T, kNsls, false>() || prepare_element_tma<N, T, kNsls, true>())
+        return -1;
     return 0;
 }
 
+
+// TMA-fed persistent kernel (SESNT_FLAG_PERSISTENT_ELEMENT); 1 when this
+// configuration has none.
+template <int N, typename T>
+int launch_element_bulk(const StepArgs<T> &a, bool sls, bool aniso, void *stream) {
+    if (sls) return aniso ? launch_element_tma<N, T, kNsls, true>(a, stream) : launch_element_tma<N, T, kNsls, false>(a, stream);
+    return aniso ? launch_element_tma<N, T, 0, true>(a, stream) : launch_element_tma<N, T, 0, false>(a, stream);
+}
 
 template <int N, typename T>
 int launch_element(const StepArgs<T> &a, bool sls, bool aniso, void *stream) {
     if constexpr (std::is_same_v<T, float>)
         if (a.contraction) return launch_element_tc<N>(a, sls, aniso, stream);
+    if (a.persistent && !a.du) {
+        const int r = launch_element_bulk<N, T>(a, sls, aniso, stream);
+        if (r <= 0) return r;
+    }
     if (sls) return aniso ? launch_element_v<N, T, kNsls, true>(a, stream) : launch_element_v<N, T, kNsls, false>(a, stream);
     return aniso ? launch_element_v<N, T, 0, true>(a, stream) : launch_element_v<N, T, 0, false>(a, stream);
 }

@@ -223,11 +223,11 @@ struct sesnt_handle {
     // After a synchronisation: the error word written by a kernel whose
     // bounded completion wait ran out (the tensor-core element kernel).
     int wait_status() {
-        if (!(g.flags & (SESNT_FLAG_TC_TF32X3 | SESNT_FLAG_TC_BF16X3))) return SESNT_OK;
+        if (!(g.flags & (SESNT_FLAG_TC_TF32X3 | SESNT_FLAG_TC_BF16X3 | SESNT_FLAG_PERSISTENT_ELEMENT))) return SESNT_OK;
         int word = 0;
         cudaError_t e = cudaMemcpy(&word, d_err, sizeof(int), cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) return cuda_fail(e, "reading the error word");
-        if (word) return fail(SESNT_ETIMEOUT, "a tensor-core completion wait ran out; the results of this run are invalid");
+        if (word) return fail(SESNT_ETIMEOUT, "a bounded completion wait of the element kernel ran out; the results of this run are invalid");
         return SESNT_OK;
     }
     int alloc(void **out, size_t bytes, const char *what) {

@@ -273,6 +273,45 @@ def test_persistent_and_simple_element_kernels_agree(gpu, sesnt_lib, lpd, n_sls,
         assert rel_l2(c, d) < 1e-12
 
 
+def test_persistent_kernel_batched(gpu, sesnt_lib):
+    """Batched simulations through the bulk-copy kernel: units are (element,
+    simulation) pairs, the state chunk of each is moved whole."""
+    wl = small_workload(4, n_sls=3, nt=120)
+    g = copy.copy(wl.grid)
+    g.batch = 3
+    srcs = []
+    for s in range(3):
+        src = copy.copy(wl.sources[0])
+        src.sim, src.lat, src.lon = s, 34.0 + s, 3.5 + 1.5 * s
+        srcs.append(src)
+    bw = workloads.Workload("batch3", g, wl.model, srcs, wl.receivers)
+    a, _, _ = run_gpu(bw, 120, fields=())
+    b, _, _ = run_gpu(with_grid(bw, flags=sesnt.FLAG_PERSISTENT_ELEMENT), 120, fields=())
+    assert np.abs(a).max() > 0
+    assert rel_l2(a, b) < 1e-5
+
+
+def test_bulk_copy_wait_runs_out_and_reports(gpu, sesnt_lib):
+    """The persistent kernel's stage waits are bounded: with the bulk loads
+    dropped they run out, the error word turns into SESNT_ETIMEOUT, and after
+    sesnt_reset the handle steps normally again."""
+    wl = small_workload(4, n_sls=3, nt=40)
+    g = with_grid(wl, flags=sesnt.FLAG_PERSISTENT_ELEMENT)
+    with sesnt.Simulation(g.grid) as sim:
+        workloads.setup(sim, g)
+        sim.set_wait_limit(64, drop_completion=True)
+        sim.run(1, 2)
+        with pytest.raises(sesnt.SesntError) as e:
+            sim.synchronize()
+        assert e.value.code == sesnt.ETIMEOUT
+        sim.set_wait_limit(1 << 22)
+        sim.reset()
+        sim.run(1, 40)
+        again = sim.seismograms()
+    fresh, _, _ = run_gpu(g, 40, fields=())
+    assert rel_l2(again, fresh) < 1e-6
+
+
 def test_kahan_update(gpu, sesnt_lib, oracle_mod):
     wl = small_workload(4, nt=300)
     k, _, _ = run_gpu(with_grid(wl, flags=sesnt.FLAG_KAHAN), 300)

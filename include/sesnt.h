@@ -242,7 +242,9 @@ int sesnt_get_seismograms(sesnt_t *h, float *out);
 /* The samples of step `it` (1..nt) of every receiver, float32
  * [batch][nrec][3] (vx, vy, vz): what receiver_cls%record(it) stores on the
  * host each step in the reference (src/config/receiver.f90:136-142).
- * Synchronous; for a Fortran driver that keeps its own traces. */
+ * Synchronous, but it waits only until step `it` is done: later steps
+ * already queued keep running while it copies (through the handle's own
+ * copy stream). For a Fortran driver that keeps its own traces. */
 int sesnt_get_samples(sesnt_t *h, int it, float *out);
 
 /* One receiver channel of simulation `sim` (SESNT_CH_*, a single bit that

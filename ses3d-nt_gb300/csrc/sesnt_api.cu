@@ -151,6 +151,14 @@ struct sesnt_handle {
     // forked from and joined back into `stream` within every enqueue
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_src = nullptr, ev_node = nullptr, ev_join = nullptr;
+    // progress marks: an event recorded after the step mark_it[q] of the
+    // current pass, so a read of step it waits for that step only; reads go
+    // through their own stream while later steps keep running
+    static constexpr int kMarks = 16;
+    cudaEvent_t mark_ev[kMarks] = {};
+    int mark_it[kMarks] = {};
+    int mark_next = 0;
+    cudaStream_t copy_stream = nullptr;
     std::string err;
     std::vector<DevBuf> bufs;
     size_t dev_bytes = 0;
@@ -254,6 +262,14 @@ struct sesnt_handle {
                 return;
             }
     }
+    void clear_marks() {
+        for (int &m : mark_it) m = -1;
+    }
+    void mark(int it) {
+        if (!mark_ev[mark_next] || cudaEventRecord(mark_ev[mark_next], stream) != cudaSuccess) return;
+        mark_it[mark_next] = it;
+        mark_next = (mark_next + 1) % kMarks;
+    }
     void drop_graph() {
         if (graph) cudaGraphExecDestroy(graph);
         graph = nullptr;
@@ -268,7 +284,10 @@ struct sesnt_handle {
         if (ev1) cudaEventDestroy(ev1);
         for (cudaEvent_t ev : {ev_fork, ev_src, ev_node, ev_join})
             if (ev) cudaEventDestroy(ev);
+        for (cudaEvent_t ev : mark_ev)
+            if (ev) cudaEventDestroy(ev);
         if (side) cudaStreamDestroy(side);
+        if (copy_stream) cudaStreamDestroy(copy_stream);
         if (stream) cudaStreamDestroy(stream);
     }
 
@@ -461,6 +480,7 @@ int zero_state(sesnt_t *h) {
         }
     h->rot_full_it = -1;
     h->last_it = 0;
+    h->clear_marks();
     return SESNT_OK;
 }
 
@@ -740,9 +760,13 @@ int run_steps(sesnt_t *h, int it0, int nsteps) {
             cudaError_t e = cudaGraphLaunch(h->graph, h->stream);
             if (e != cudaSuccess) return h->cuda_fail(e, "cudaGraphLaunch");
             left -= kGraphSteps;
+            h->mark(it0 + nsteps - left - 1);
         }
     }
-    if (left > 0 && (rc = enqueue_steps<T>(h, left))) return rc;
+    if (left > 0) {
+        if ((rc = enqueue_steps<T>(h, left))) return rc;
+        h->mark(it0 + nsteps - 1);
+    }
     h->last_it = it0 + nsteps - 1;
     if (h->g.flags & SESNT_FLAG_ROTATION) h->rot_full_it = h->last_it;
     return SESNT_OK;
@@ -857,6 +881,7 @@ int run_impl(sesnt_t *h, int it0, int nsteps) {
         return h->fail(SESNT_ERANGE, "steps %d..%d outside 1..nt=%d", it0, it0 + nsteps - 1, h->g.nt);
     int rc;
     if ((rc = prepare_run<T>(h))) return rc;
+    if (it0 <= h->last_it) h->clear_marks();  // a step again: earlier marks no longer say "done"
     if (h->snaps.empty()) return run_steps<T>(h, it0, nsteps);
     const int last = it0 + nsteps - 1;
     int it = it0;
@@ -868,6 +893,7 @@ int run_impl(sesnt_t *h, int it0, int nsteps) {
         for (const auto &q : h->snaps) rot = rot || (is_rotation(q.which) && snapshot_due(q, due));
         k_set_it<<<1, 1, 0, h->stream>>>(h->d_it, due);
         if ((rc = enqueue_steps<T>(h, 1, rot))) return rc;
+        h->mark(due);
         h->last_it = due;
         if (rot || (h->g.flags & SESNT_FLAG_ROTATION)) h->rot_full_it = due;
         if ((rc = capture_snapshots<T>(h, due))) return rc;
@@ -1120,6 +1146,10 @@ int sesnt_create(const sesnt_grid_t *grid, sesnt_t **out) {
     cudaEventCreate(&h->ev0);
     cudaEventCreate(&h->ev1);
     e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking);
+    for (cudaEvent_t &ev : h->mark_ev)
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+    h->clear_marks();
     for (cudaEvent_t *ev : {&h->ev_fork, &h->ev_src, &h->ev_node, &h->ev_join})
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
     if (e != cudaSuccess) {
@@ -1365,10 +1395,18 @@ int sesnt_get_samples(sesnt_t *h, int it, float *out) {
     if (h->rec_dirty) return h->fail(SESNT_ESTATE, "receivers added after the last step");
     const size_t E = h->esize, nt = h->g.nt;
     std::vector<double> tmp(h->S * nrec * 3);
+    // wait for step it only (the earliest progress mark at or after it), or
+    // for everything queued when no mark covers it
+    int best = -1;
+    for (int q = 0; q < sesnt_handle::kMarks; ++q)
+        if (h->mark_it[q] >= it && (best < 0 || h->mark_it[q] < h->mark_it[best])) best = q;
+    cudaStream_t cs = best >= 0 ? h->copy_stream : h->stream;
+    cudaError_t e = best >= 0 ? cudaEventSynchronize(h->mark_ev[best]) : cudaSuccess;
     // one strided 2-D copy: rows [s][r][c] of the seismogram array, column it-1
-    cudaError_t e = cudaMemcpy2DAsync(tmp.data(), E, (const char *)h->d_seis + (size_t)(it - 1) * E, nt * E, E,
-                                      (size_t)h->S * nrec * 3, cudaMemcpyDeviceToHost, h->stream);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpy2DAsync(tmp.data(), E, (const char *)h->d_seis + (size_t)(it - 1) * E, nt * E, E,
+                              (size_t)h->S * nrec * 3, cudaMemcpyDeviceToHost, cs);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
     if (e != cudaSuccess) return h->cuda_fail(e, "reading samples");
     for (size_t x = 0; x < tmp.size(); ++x) {
         const size_t r = (x / 3) % nrec;

@@ -291,6 +291,28 @@ def test_persistent_kernel_batched(gpu, sesnt_lib):
     assert rel_l2(a, b) < 1e-5
 
 
+def test_samples_read_while_later_steps_run(gpu, sesnt_lib):
+    """sesnt_get_samples(it) waits for step it only: samples of one run read
+    while the next run is queued equal the recorded seismograms, also after a
+    reset and a second pass."""
+    wl = small_workload(4, nt=100)
+    with sesnt.Simulation(wl.grid) as sim:
+        workloads.setup(sim, wl)
+        for _ in range(2):
+            got = np.zeros((100, 1, len(wl.receivers), 3), np.float32)
+            sim.run(1, 32)
+            sim.run(33, 32)
+            for it in range(1, 33):
+                sim.samples(it, got[it - 1])
+            sim.run(65, 36)
+            for it in range(33, 101):
+                sim.samples(it, got[it - 1])
+            seis = sim.seismograms()
+            assert np.abs(seis).max() > 0
+            assert np.array_equal(np.moveaxis(got, 0, -1), seis)
+            sim.reset()
+
+
 def test_bulk_copy_wait_runs_out_and_reports(gpu, sesnt_lib):
     """The persistent kernel's stage waits are bounded: with the bulk loads
     dropped they run out, the error word turns into SESNT_ETIMEOUT, and after

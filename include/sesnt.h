@@ -247,6 +247,18 @@ int sesnt_get_seismograms(sesnt_t *h, float *out);
  * copy stream). For a Fortran driver that keeps its own traces. */
 int sesnt_get_samples(sesnt_t *h, int it, float *out);
 
+/* Checkpoint and resume (no counterpart in the reference, which keeps no
+ * restartable state). sesnt_state_bytes gives the size of the host buffer;
+ * sesnt_save_state copies the time-stepping state into it: velocity,
+ * stress, memory variables, Kahan compensation, displacement gradient, the
+ * recorded traces and the last step. sesnt_load_state restores it into a
+ * handle with the same grid, precision, flags and receivers (model and
+ * sources are not part of the state), after which stepping continues at
+ * the saved step + 1. Synchronous. */
+long long sesnt_state_bytes(sesnt_t *h);
+int sesnt_save_state(sesnt_t *h, void *buf);
+int sesnt_load_state(sesnt_t *h, const void *buf);
+
 /* One receiver channel of simulation `sim` (SESNT_CH_*, a single bit that
  * was requested for that receiver), float32 [nt]. Synchronous. No single
  * counterpart in the reference: channel_cls%data of one receiver channel

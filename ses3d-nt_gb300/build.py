@@ -40,19 +40,23 @@ def sources():
     return cu, cpp
 
 
-def build(verbose=False, extra_nvcc=()):
-    """Compile every translation unit and link libsesnt.so. Returns its path."""
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose=False, extra_nvcc=(), out_dir=None):
+    """Compile every translation unit and link libsesnt.so. Returns its path.
+    out_dir: build a separate library there (objects and libsesnt.so, no
+    CLI), e.g. the bounds-check build with extra_nvcc=["-DSESNT_BOUNDS_CHECK"]."""
+    build_dir = os.path.join(out_dir, "_build") if out_dir else BUILD
+    lib = os.path.join(out_dir, "libsesnt.so") if out_dir else LIB
+    os.makedirs(build_dir, exist_ok=True)
     nvcc = _nvcc()
     cu, cpp = sources()
     jobs = []
     for f in cu:
-        obj = os.path.join(BUILD, f + ".o")
+        obj = os.path.join(build_dir, f + ".o")
         jobs.append(([nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-I", INCLUDE,
                       "-Xcompiler", "-fPIC,-ffp-contract=off", *extra_nvcc,
                       "-c", os.path.join(CSRC, f), "-o", obj], obj))
     for f in cpp:
-        obj = os.path.join(BUILD, f + ".o")
+        obj = os.path.join(build_dir, f + ".o")
         jobs.append((["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall",
                       "-I", INCLUDE, "-I", "/usr/local/cuda/include",
                       "-c", os.path.join(CSRC, f), "-o", obj], obj))
@@ -63,8 +67,10 @@ def build(verbose=False, extra_nvcc=()):
             if o.strip():
                 print(o)
     objs = [o for _, o in jobs]
-    _run([nvcc, *ARCH, "-shared", "-o", LIB + ".tmp", *objs, "-Xcompiler", "-fPIC"])
-    os.replace(LIB + ".tmp", LIB)
+    _run([nvcc, *ARCH, "-shared", "-o", lib + ".tmp", *objs, "-Xcompiler", "-fPIC"])
+    os.replace(lib + ".tmp", lib)
+    if out_dir:
+        return lib
     # command-line driver linked against the library (found next to it)
     _run(["g++", "-O2", "-std=c++17", "-o", CLI + ".tmp", os.path.join(HERE, "cli", "ses3d-nt-gpu.cpp"),
           "-L" + HERE, "-lsesnt", "-Wl,-rpath,$ORIGIN"])

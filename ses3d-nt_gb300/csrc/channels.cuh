@@ -24,6 +24,7 @@ __global__ void __launch_bounds__(((N + 1) * (N + 1) * (N + 1) + 31) / 32 * 32)
     __shared__ T sv[3 * NP];
     const int idx = blockIdx.x, s = blockIdx.y, t = threadIdx.x;
     const int e = elems ? elems[idx] : idx;
+    if (!in_range(e, a.nel, a.err)) return;  // whole block
     for (int x = t; x < 3 * P * P; x += blockDim.x) sD[x] = a.tabD[x];
     const int p = t;
     const bool act = p < NP;
@@ -121,6 +122,7 @@ __device__ __forceinline__ void record_extra(const StepArgs<T> &a, int r, int s,
     const unsigned xm = a.rec_xmask[r];
     if (!xm) return;
     int slot = a.rec_xslot[r];
+    if (!in_range(slot + __popc(xm) - 1, a.nxtr, a.err)) return;  // whole warp
     T *xo = a.xseis + (size_t)s * a.nxtr * a.nt + (it - 1);
     const size_t nuni = (size_t)a.nuni;
     auto reduce = [](T x) {
@@ -130,6 +132,7 @@ __device__ __forceinline__ void record_extra(const StepArgs<T> &a, int r, int s,
     };
     if (xm & (SESNT_CH_ROT_VX | SESNT_CH_ROT_VY | SESNT_CH_ROT_VZ)) {
         const int rr = a.rec_rot[r];
+        if (!in_range(rr, a.nrot, a.err)) return;
         const T *vs = a.v + (size_t)s * 3 * nuni;
         for (int c = 0; c < 3; ++c) {
             if (!(xm & (SESNT_CH_ROT_VX << c))) continue;
@@ -151,9 +154,9 @@ __device__ __forceinline__ void record_extra(const StepArgs<T> &a, int r, int s,
     for (int c = 0; c < 9; ++c) {
         if (!(xm & (SESNT_CH_MXX << c))) continue;
         T acc = 0;
-        if (ri >= 0) {
+        if (ri >= 0 && in_range(ri, a.nsrc, a.err)) {
             const SrcRec rec = a.src[ri];
-            if (rec.vm[c] >= 0) {
+            if (rec.vm[c] >= 0 && in_range(rec.vm[c], a.n_src_vm, a.err) && in_range(rec.data[c], a.n_src_data, a.err)) {
                 const T d = a.src_data[(size_t)rec.data[c] * a.nt + (it - 1)];
                 const T *svm = a.src_vm + (size_t)rec.vm[c] * NP;
                 for (int p = lane; p < NP; p += 32) {

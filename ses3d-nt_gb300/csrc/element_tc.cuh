@@ -212,7 +212,8 @@ __global__ void __launch_bounds__(TcCfg<N, PREC>::NT) k_element_tc(const StepArg
     constexpr int NPS = state_stride(NP);  // element-blocked [e][s][comp][NPS]
     T *sig = a.sig + ((size_t)e * S + s) * 6 * NPS + p;
     T *mem = a.mem + ((size_t)e * S + s) * 6 * MS * NPS + p;
-    if (act) {
+    if (act && in_range(unique_index<N>(a.NXU, a.NYU, ex, ey, ez, i, j, k), nuni, a.err) &&
+        in_range(li, nloc, a.err)) {
         u = unique_index<N>(a.NXU, a.NYU, ex, ey, ez, i, j, k);
         const T *vs = a.v + (size_t)s * 3 * nuni;
         vx = vs[u];

@@ -141,6 +141,7 @@ __global__ void __launch_bounds__(TmaCfg<N, T, NSLS>::NT, TmaCfg<N, T, NSLS>::MI
         const int e = (int)(g / S), s = (int)(g % S);
         const int ex = e % a.nx, ey = (e / a.nx) % a.ny, ez = e / (a.nx * a.ny);
         const size_t u = unique_index<N>(a.NXU, a.NYU, ex, ey, ez, i, j, k3);
+        if (!in_range(u, nuni, a.err) || !in_range((size_t)e * NP + p, nloc, a.err)) return;
         const T *vs = a.v + (size_t)s * 3 * nuni;
         nv[0] = vs[u];
         nv[1] = vs[nuni + u];

@@ -64,6 +64,22 @@ struct ElemCfg {
                               : (NT <= 256 ? SESNT_MINB_256 : (NT <= 384 ? SESNT_MINB_384 : (NT <= 512 ? 2 : 1)));
 };
 
+// Bounds-check builds (-DSESNT_BOUNDS_CHECK): a global index outside its
+// buffer sets bit 2 of the error word and the access is skipped; no device
+// assert, no trap. In normal builds the check compiles away.
+__device__ __forceinline__ bool in_range(size_t idx, size_t n, int *err) {
+#ifdef SESNT_BOUNDS_CHECK
+    if (idx < n) return true;
+    atomicOr(err, 2);
+    return false;
+#else
+    (void)idx;
+    (void)n;
+    (void)err;
+    return true;
+#endif
+}
+
 // Evict-first hints: measured faster on the stores only (loads without the
 // hint keep the next blocks' shared velocity lines warm).
 #ifndef SESNT_HINT_LOADS
@@ -331,7 +347,7 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::M
     const int le = t / NP;
     const int p = t - le * NP;
     const int e = g * EPB + le;
-    const bool act = (le < EPB) && (e < a.nel);
+    bool act = (le < EPB) && (e < a.nel);
     const int i = p % P, j = (p / P) % P, k = p / (P * P);
     int ex = 0, ey = 0, ez = 0;
     size_t u = 0;
@@ -347,6 +363,10 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::M
     const size_t sb = (size_t)e * S + s;
     T *sig = a.sig + sb * 6 * NPS + p;
     T *mem = a.mem + sb * 6 * MS * NPS + p;
+    act = act && in_range(unique_index<N>(a.NXU, a.NYU, e % a.nx, (e / a.nx) % a.ny, e / (a.nx * a.ny), i, j, k),
+                          nuni, a.err) &&
+          in_range(li, nloc, a.err) && in_range(sb * 6 * NPS + 5 * NPS + p, (size_t)a.nel * S * 6 * NPS, a.err) &&
+          (NSLS == 0 || in_range(sb * 6 * MS * NPS + (6 * MS - 1) * NPS + p, (size_t)a.nel * S * 6 * MS * NPS, a.err));
     if (act) {
         ex = e % a.nx;
         ey = (e / a.nx) % a.ny;
@@ -409,10 +429,12 @@ __global__ void __launch_bounds__(((ElemCfg<N>::NP + 31) / 32) * 32) k_sources(c
     const int t = threadIdx.x;
     for (int x = t; x < P * P; x += blockDim.x) sD[x] = a.tabD[3 * P * P + x];
     const int p = t;
-    const bool act = p < NP;
     const int i = p % P, j = (p / P) % P, k = p / (P * P);
     const int e = rec.elem;
     const int ex = e % a.nx, ey = (e / a.nx) % a.ny, ez = e / (a.nx * a.ny);
+    bool act = p < NP && in_range(e, a.nel, a.err) && in_range(rec.sim, a.S, a.err) && in_range(di, a.nt, a.err);
+    for (int c = 0; c < 9 && act; ++c)
+        act = rec.vm[c] < 0 || (in_range(rec.vm[c], a.n_src_vm, a.err) && in_range(rec.data[c], a.n_src_data, a.err));
     T f0[3] = {0, 0, 0};
     if (act) {
         const T rr = a.r[ez * P + k];
@@ -534,6 +556,7 @@ __global__ void __launch_bounds__(128) k_receivers(const StepArgs<T> a) {
     if (r >= a.nrec) return;
     const int it = *a.d_it + a.step_off;
     const int e = a.rec_elem[r];
+    if (!in_range(e, a.nel, a.err) || !in_range(it - 1, a.nt, a.err)) return;  // whole warp
     const int ex = e % a.nx, ey = (e / a.nx) % a.ny, ez = e / (a.nx * a.ny);
     const size_t nuni = (size_t)a.nuni;
     const T *vs = a.v + (size_t)s * 3 * nuni;

@@ -15,6 +15,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/sesnt.h"
 #include "sesnt_internal.h"
 #include "snapshot_writer.h"
@@ -51,6 +53,13 @@ const LpdOps<double> *lpd_ops<double>(int lpd) {
 namespace {
 
 thread_local std::string g_create_error;
+
+// NVTX range over one API call (visible in Nsight timelines; a no-op
+// without a profiler attached).
+struct Range {
+    explicit Range(const char *name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+};
 
 __global__ void k_set_it(int *d_it, int v) { *d_it = v; }
 
@@ -177,7 +186,7 @@ struct sesnt_handle {
     std::vector<HostSource> sources;
     bool src_dirty = true;
     void *d_src = nullptr, *d_src_vm = nullptr, *d_src_data = nullptr;
-    int nsrc_rec = 0;
+    int nsrc_rec = 0, n_src_vm = 0, n_src_data = 0;
     std::vector<int> rec_elem;
     std::vector<float> rec_vm;
     std::vector<unsigned> rec_mask;
@@ -231,10 +240,13 @@ struct sesnt_handle {
     // After a synchronisation: the error word written by a kernel whose
     // bounded completion wait ran out (the tensor-core element kernel).
     int wait_status() {
+#ifndef SESNT_BOUNDS_CHECK
         if (!(g.flags & (SESNT_FLAG_TC_TF32X3 | SESNT_FLAG_TC_BF16X3 | SESNT_FLAG_PERSISTENT_ELEMENT))) return SESNT_OK;
+#endif
         int word = 0;
         cudaError_t e = cudaMemcpy(&word, d_err, sizeof(int), cudaMemcpyDeviceToHost);
         if (e != cudaSuccess) return cuda_fail(e, "reading the error word");
+        if (word & 2) return fail(SESNT_ERANGE, "bounds check: a kernel index was outside its buffer");
         if (word) return fail(SESNT_ETIMEOUT, "a bounded completion wait of the element kernel ran out; the results of this run are invalid");
         return SESNT_OK;
     }
@@ -309,7 +321,7 @@ struct sesnt_handle {
         a.lam = (const T *)lam; a.mu = (const T *)mu; a.A = (const T *)A; a.B = (const T *)B; a.C = (const T *)C;
         a.tau = (const T *)tau;
         a.sig = (T *)sig; a.mem = (T *)mem; a.v = (T *)v; a.vc = (T *)vc; a.F = (T *)F; a.invM = (const T *)invM;
-        a.nsrc = nsrc_rec; a.nt = g.nt; a.src = (const SrcRec *)d_src; a.src_vm = (const T *)d_src_vm;
+        a.nsrc = nsrc_rec; a.nt = g.nt; a.n_src_vm = n_src_vm; a.n_src_data = n_src_data; a.src = (const SrcRec *)d_src; a.src_vm = (const T *)d_src_vm;
         a.src_data = (const T *)d_src_data;
         a.nrec = nrec_dev; a.rec_elem = d_rec_elem; a.rec_vm = (const T *)d_rec_vm; a.seis = (T *)d_seis;
         a.d_it = d_it; a.step_off = 0;
@@ -528,7 +540,6 @@ int upload_sources(sesnt_t *h) {
                 r->data[c] = data_row[s][c];
             }
     }
-    (void)nvm;
     int rc;
     if ((rc = h->alloc(&h->d_src, recs.size() * sizeof(SrcRec), "source records"))) return rc;
     if ((rc = h->alloc(&h->d_src_vm, vm.size() * sizeof(T), "source weights"))) return rc;
@@ -540,6 +551,8 @@ int upload_sources(sesnt_t *h) {
         e = cudaMemcpy(h->d_src_data, data.data(), data.size() * sizeof(T), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return h->cuda_fail(e, "uploading sources");
     h->nsrc_rec = (int)recs.size();
+    h->n_src_vm = nvm;
+    h->n_src_data = ndata;
     return SESNT_OK;
 }
 
@@ -849,6 +862,7 @@ int field_source(sesnt_t *h, int sim, int which, T *scratch, const T **out, bool
 // behind the step's kernels and queue it for the writer thread.
 template <typename T>
 int capture_snapshots(sesnt_t *h, int it) {
+    Range r("snapshot capture");
     for (const auto &q : h->snaps) {
         if (!snapshot_due(q, it)) continue;
         const T *src = nullptr;
@@ -1108,6 +1122,7 @@ size_t footprint(const sesnt_grid_t *g, bool aniso) {
 extern "C" {
 
 int sesnt_create(const sesnt_grid_t *grid, sesnt_t **out) {
+    Range r("sesnt_create");
     if (!out) {
         g_create_error = "out is NULL";
         return SESNT_EINVAL;
@@ -1229,6 +1244,7 @@ const char *sesnt_last_error(const sesnt_t *h) {
 int sesnt_set_model(sesnt_t *h, const float *rhoinv, const float *lambda, const float *mu, const float *a,
                     const float *b, const float *c, const float *q) {
     if (!h) return SESNT_EINVAL;
+    Range r("sesnt_set_model");
     if (!rhoinv || !lambda || !mu) return h->fail(SESNT_EINVAL, "rhoinv, lambda and mu are required");
     return h->dbl ? set_model_impl<double>(h, rhoinv, lambda, mu, a, b, c, q)
                   : set_model_impl<float>(h, rhoinv, lambda, mu, a, b, c, q);
@@ -1308,6 +1324,7 @@ int sesnt_add_receiver(sesnt_t *h, int ex, int ey, int ez, const float *vanderm,
 
 int sesnt_step(sesnt_t *h, int it) {
     if (!h) return SESNT_EINVAL;
+    Range r("sesnt_step");
     const bool g = h->use_graph;
     h->use_graph = false;
     int rc = run_any(h, it, 1);
@@ -1317,6 +1334,7 @@ int sesnt_step(sesnt_t *h, int it) {
 
 int sesnt_run(sesnt_t *h, int it0, int nsteps) {
     if (!h) return SESNT_EINVAL;
+    Range r("sesnt_run");
     return run_any(h, it0, nsteps);
 }
 
@@ -1389,6 +1407,7 @@ int sesnt_run_profiled(sesnt_t *h, int it0, int nsteps, float ms[4]) {
 
 int sesnt_get_samples(sesnt_t *h, int it, float *out) {
     if (!h || !out) return SESNT_EINVAL;
+    Range r("sesnt_get_samples");
     if (it < 1 || it > h->g.nt) return h->fail(SESNT_ERANGE, "step %d outside 1..%d", it, h->g.nt);
     const size_t nrec = h->rec_elem.size();
     if (nrec == 0) return SESNT_OK;
@@ -1446,11 +1465,13 @@ int sesnt_set_wait_limit(sesnt_t *h, int polls, int drop_completion) {
 
 int sesnt_get_seismograms(sesnt_t *h, float *out) {
     if (!h || !out) return SESNT_EINVAL;
+    Range r("sesnt_get_seismograms");
     return h->dbl ? get_seis_impl<double>(h, out) : get_seis_impl<float>(h, out);
 }
 
 int sesnt_get_field(sesnt_t *h, int sim, int which, void *out, int out_precision) {
     if (!h || !out) return SESNT_EINVAL;
+    Range r("sesnt_get_field");
     if (sim < 0 || sim >= h->S) return h->fail(SESNT_ERANGE, "simulation %d outside 0..%d", sim, h->S - 1);
     if (out_precision != 4 && out_precision != 8) return h->fail(SESNT_EINVAL, "out_precision must be 4 or 8");
     if (!h->model_set && which != SESNT_FIELD_TAPER)
@@ -1491,6 +1512,94 @@ long long sesnt_footprint_bytes(const sesnt_grid_t *grid) {
 }
 
 void *sesnt_stream(const sesnt_t *h) { return h ? (void *)h->stream : nullptr; }
+
+namespace {
+// Checkpoint layout: a fixed header, then the state buffers in this order.
+struct StateHeader {
+    char magic[8];
+    int nx, ny, nz, lpd, batch, precision, n_sls, nrec, nxtr, last_it;
+    unsigned flags;
+    int pad;
+};
+
+std::vector<std::pair<void *, size_t>> state_buffers(sesnt_t *h) {
+    const size_t E = h->esize, S = h->S, NPS = state_stride(h->NP), nel = h->nel, nuni = h->nuni;
+    std::vector<std::pair<void *, size_t>> b = {{h->v, 3 * nuni * E * S}, {h->sig, 6 * nel * NPS * E * S}};
+    if (h->mem) b.push_back({h->mem, 6 * kNsls * nel * NPS * E * S});
+    if (h->vc) b.push_back({h->vc, 3 * nuni * E * S});
+    if (h->du) b.push_back({h->du, 9 * (size_t)h->nloc * E * S});
+    if (h->d_seis) b.push_back({h->d_seis, S * h->rec_elem.size() * 3 * (size_t)h->g.nt * E});
+    if (h->d_xseis) b.push_back({h->d_xseis, S * (size_t)h->nxtr * h->g.nt * E});
+    return b;
+}
+
+int prepare_receivers(sesnt_t *h) {
+    if (!h->rec_dirty) return SESNT_OK;
+    int rc = h->dbl ? upload_receivers<double>(h) : upload_receivers<float>(h);
+    return rc ? rc : upload_receiver_sources(h);
+}
+
+StateHeader state_header(const sesnt_t *h) {
+    StateHeader hd{};
+    std::memcpy(hd.magic, "SESNTST1", 8);
+    hd.nx = h->g.nx; hd.ny = h->g.ny; hd.nz = h->g.nz; hd.lpd = h->g.lpd; hd.batch = h->S;
+    hd.precision = h->g.precision; hd.n_sls = h->g.n_sls; hd.nrec = (int)h->rec_elem.size(); hd.nxtr = h->nxtr;
+    hd.flags = h->g.flags & (SESNT_FLAG_KAHAN | SESNT_FLAG_STRAIN);
+    hd.last_it = h->last_it;
+    return hd;
+}
+}  // namespace
+
+long long sesnt_state_bytes(sesnt_t *h) {
+    if (!h) return SESNT_EINVAL;
+    int rc = prepare_receivers(h);
+    if (rc) return rc;
+    long long n = sizeof(StateHeader);
+    for (auto &b : state_buffers(h)) n += (long long)b.second;
+    return n;
+}
+
+int sesnt_save_state(sesnt_t *h, void *buf) {
+    if (!h || !buf) return SESNT_EINVAL;
+    int rc = prepare_receivers(h);
+    if (rc) return rc;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "synchronize");
+    if ((rc = h->wait_status())) return rc;
+    const StateHeader hd = state_header(h);
+    char *o = (char *)buf;
+    std::memcpy(o, &hd, sizeof hd);
+    o += sizeof hd;
+    for (auto &b : state_buffers(h)) {
+        if ((e = cudaMemcpy(o, b.first, b.second, cudaMemcpyDeviceToHost)) != cudaSuccess)
+            return h->cuda_fail(e, "saving state");
+        o += b.second;
+    }
+    return SESNT_OK;
+}
+
+int sesnt_load_state(sesnt_t *h, const void *buf) {
+    if (!h || !buf) return SESNT_EINVAL;
+    int rc = prepare_receivers(h);
+    if (rc) return rc;
+    StateHeader hd, want = state_header(h);
+    std::memcpy(&hd, buf, sizeof hd);
+    want.last_it = hd.last_it;
+    if (std::memcmp(&hd, &want, sizeof hd) != 0)
+        return h->fail(SESNT_EINVAL, "state was saved from a handle with another grid, precision, flags or receivers");
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "synchronize");
+    const char *in = (const char *)buf + sizeof hd;
+    for (auto &b : state_buffers(h)) {
+        if ((e = cudaMemcpy(b.first, in, b.second, cudaMemcpyHostToDevice)) != cudaSuccess)
+            return h->cuda_fail(e, "loading state");
+        in += b.second;
+    }
+    h->last_it = hd.last_it;
+    h->rot_full_it = -1;
+    h->clear_marks();
+    return SESNT_OK;
+}
 
 int sesnt_get_trace(sesnt_t *h, int sim, int receiver, unsigned channel, float *out) {
     if (!h || !out) return SESNT_EINVAL;

@@ -66,6 +66,7 @@ struct StepArgs {
     const T *invM;
     // sources
     int nsrc, nt;
+    int n_src_vm, n_src_data;  // rows of src_vm and src_data (bounds-check builds)
     const SrcRec *src;
     const T *src_vm;    // [n_vm][NP]
     const T *src_data;  // [n_data][nt]

@@ -19,7 +19,8 @@ from dataclasses import dataclass
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libsesnt.so")
+# SESNT_LIBRARY selects another build of the library (e.g. the bounds-check build)
+LIB_PATH = os.environ.get("SESNT_LIBRARY") or os.path.join(HERE, "libsesnt.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "sesnt.h")
 
 OK = 0
@@ -177,6 +178,9 @@ def lib():
         "sesnt_forward": (I, [C.c_char_p, I, C.POINTER(C.c_int)]),
         "sesnt_get_trace": (I, [P, I, I, U, fp]),
         "sesnt_set_wait_limit": (I, [P, I, I]),
+        "sesnt_state_bytes": (C.c_longlong, [P]),
+        "sesnt_save_state": (I, [P, P]),
+        "sesnt_load_state": (I, [P, P]),
         "sesnt_add_snapshot": (I, [P, I, I, I, I, I, C.c_char_p, C.c_char_p, I]),
         "sesnt_snapshots_wait": (I, [P]),
         "sesnt_field_name": (C.c_char_p, [I]),
@@ -311,6 +315,17 @@ class Simulation:
 
     def synchronize(self):
         self._c(lib().sesnt_synchronize(self._h))
+
+    def save_state(self):
+        """Checkpoint of the time-stepping state (bytes)."""
+        n = self._c(lib().sesnt_state_bytes(self._h))
+        buf = np.zeros(n, np.uint8)
+        self._c(lib().sesnt_save_state(self._h, buf.ctypes.data_as(C.c_void_p)))
+        return buf
+
+    def load_state(self, buf):
+        buf = np.ascontiguousarray(buf, np.uint8)
+        self._c(lib().sesnt_load_state(self._h, buf.ctypes.data_as(C.c_void_p)))
 
     def set_wait_limit(self, polls, drop_completion=False):
         self._c(lib().sesnt_set_wait_limit(self._h, polls, 1 if drop_completion else 0))

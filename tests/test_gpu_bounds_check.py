@@ -1,0 +1,80 @@
+"""The bounds-check build (-DSESNT_BOUNDS_CHECK): every global index of the
+step kernels is checked against its buffer; an index out of range sets a bit
+of the handle's error word (no device assert, no trap), which the next
+synchronising call returns as SESNT_ERANGE. This is the stand-in for a
+memory sanitizer: the library is rebuilt with the checks, and a subprocess
+runs every kernel variant (degrees 2-7, elastic and SLS, anisotropy,
+batches, the persistent and tensor-core element kernels, strain and rotation
+state, every receiver channel, snapshot fields) on small grids."""
+import os
+import subprocess
+import sys
+
+import pytest
+
+import build
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(os.path.dirname(HERE), "ses3d-nt_gb300")
+
+SCRIPT = r"""
+import sys
+sys.path[:0] = [%r, %r]
+import numpy as np
+import sesnt, workloads
+from test_gpu_parity import small_workload, with_grid
+
+ALL = 0xFFFF
+cases = [  # lpd, n_sls, aniso, kind, flags, batch
+    (2, 0, False, sesnt.SOURCE_MT, 0, 1),
+    (3, 3, False, sesnt.SOURCE_SF, 0, 2),
+    (4, 3, True, sesnt.SOURCE_MT, sesnt.FLAG_STRAIN | sesnt.FLAG_ROTATION, 2),
+    (4, 3, False, sesnt.SOURCE_MT, sesnt.FLAG_PERSISTENT_ELEMENT, 3),
+    (4, 0, True, sesnt.SOURCE_SF, sesnt.FLAG_TC_TF32X3, 1),
+    (5, 0, False, sesnt.SOURCE_MT, sesnt.FLAG_KAHAN, 1),
+    (6, 3, False, sesnt.SOURCE_MT, sesnt.FLAG_TC_BF16X3, 1),
+    (7, 0, True, sesnt.SOURCE_MT, sesnt.FLAG_PERSISTENT_ELEMENT, 1),
+]
+for lpd, n_sls, aniso, kind, flags, batch in cases:
+    wl = small_workload(lpd, n_sls=n_sls, aniso=aniso, kind=kind, nt=40)
+    src = wl.sources[0]
+    wl.receivers.insert(0, workloads.Receiver(lat=src.lat, lon=src.lon, depth=src.depth))
+    g = with_grid(wl, flags=flags, batch=batch).grid
+    with sesnt.Simulation(g) as sim:
+        m = wl.model
+        sim.set_model(m["rhoinv"], m["lambda"], m["mu"], m.get("a"), m.get("b"), m.get("c"), m.get("q"))
+        for s in range(batch):
+            elem, vm = sesnt.locate_point(g, src.lat, src.lon, src.depth)
+            stf = sesnt.source_signature(src.wavelet, src.onset, src.width, g.dt, g.nt)
+            sim.add_source(s, elem, vm, kind, np.asarray(src.comp, np.float32), stf)
+        for r in wl.receivers:
+            elem, vm = sesnt.locate_point(g, r.lat, r.lon, r.depth)
+            sim.add_receiver(elem, vm, ALL)
+        sim.add_snapshot("pressure", 10, 10, 30, prefix=%r + "/", attribute="p%%d_%%d" %% (lpd, flags))
+        sim.run(1, 40)
+        sim.synchronize()
+        sim.wait_snapshots()
+        for name in ("vz", "sxy", "pressure"):
+            sim.field(name, sim=batch - 1)
+        if flags & sesnt.FLAG_STRAIN:
+            sim.field("exy")
+        if flags & sesnt.FLAG_ROTATION:
+            sim.field("rot_vz")
+        for b in range(16):
+            sim.trace(0, 1 << b, sim=batch - 1)
+        sim.synchronize()
+    print("case", lpd, n_sls, aniso, kind, flags, batch, "clean")
+print("OK", len(cases))
+"""
+
+
+def test_every_kernel_in_bounds(gpu, tmp_path):
+    lib_dir = tmp_path / "bounds-check"
+    build.build(extra_nvcc=["-DSESNT_BOUNDS_CHECK"], out_dir=str(lib_dir))
+    env = dict(os.environ, SESNT_LIBRARY=str(lib_dir / "libsesnt.so"))
+    code = SCRIPT % (PKG, HERE, str(tmp_path))
+    r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
+    assert "OK 8" in r.stdout

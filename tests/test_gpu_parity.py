@@ -409,3 +409,29 @@ def test_model_validation(gpu, sesnt_lib):
         q = np.full(wl.grid.shape, 100.0, np.float32)
         with pytest.raises(sesnt.SesntError):
             sim.set_model(m["rhoinv"], m["lambda"], m["mu"], q=q)  # elastic handle, q given
+
+
+@pytest.mark.parametrize("flags", [0, sesnt.FLAG_KAHAN | sesnt.FLAG_STRAIN])
+def test_checkpoint_and_resume(gpu, sesnt_lib, flags):
+    """A state saved after step 60 and loaded into a fresh handle continues
+    to the same seismograms and wavefields as the uninterrupted run."""
+    wl = with_grid(small_workload(4, n_sls=3, nt=120), flags=flags)
+    with sesnt.Simulation(wl.grid) as sim:
+        workloads.setup(sim, wl)
+        sim.run(1, 60)
+        ck = sim.save_state()
+        sim.run(61, 60)
+        a, fa = sim.seismograms(), sim.field("vz")
+    with sesnt.Simulation(wl.grid) as sim:
+        workloads.setup(sim, wl)
+        sim.load_state(ck)
+        sim.run(61, 60)
+        b, fb = sim.seismograms(), sim.field("vz")
+    assert np.abs(a).max() > 0
+    assert rel_l2(b, a) < 1e-5 and rel_l2(fb, fa) < 1e-5
+    other = with_grid(small_workload(4, n_sls=3, nt=120, nx=7), flags=flags)
+    with sesnt.Simulation(other.grid) as sim:
+        workloads.setup(sim, other)
+        with pytest.raises(sesnt.SesntError) as e:
+            sim.load_state(ck)
+        assert e.value.code == sesnt.EINVAL

@@ -9,6 +9,8 @@
 // steps on its own CUDA stream, so the work of requests that arrive while
 // others run overlaps on the device. A batch that has run all its steps
 // hands its seismograms back, frees its memory and makes room for the next.
+// Handles are created and loaded (model upload, precompute) by a set-up
+// thread, so the scheduler keeps launching the running batches meanwhile.
 // Latency is measured from submission to the last batch's completion.
 #include <cuda_runtime.h>
 
@@ -57,6 +59,7 @@ struct Batch {
     int it = 1;  // next step
     cudaEvent_t ev = nullptr;
     bool in_flight = false;
+    bool ready = false;  // handle created and loaded by the set-up thread
 };
 
 }  // namespace
@@ -70,7 +73,9 @@ struct sesnt_server {
     std::vector<std::unique_ptr<Batch>> active;
     long long next_id = 1, used_bytes = 0, budget = 0;
     std::atomic<bool> stop{false};
-    std::thread worker;
+    std::thread worker, setup;
+    std::deque<Batch *> setup_queue;
+    std::condition_variable cv_setup;
     int device = 0;
     // statistics
     std::vector<double> latencies, queue_waits;
@@ -81,8 +86,11 @@ struct sesnt_server {
     std::string err;
 
     void run();
+    void run_setup();
     bool admit_locked();
     void finish_batch(Batch *b);
+    void request_settled_locked(Request *r, const Batch *gone);
+    void remove_active_locked(const Batch *b);
 };
 
 namespace {
@@ -101,7 +109,7 @@ bool sesnt_server::admit_locked() {
     bool any_started = false;
     for (auto it = queue.begin(); it != queue.end() && (int)active.size() < cfg.max_active;) {
         Request *r = *it;
-        if (r->cancelled) {
+        if (r->cancelled || r->failed) {
             it = queue.erase(it);
             continue;
         }
@@ -118,35 +126,6 @@ bool sesnt_server::admit_locked() {
         b->src0 = r->next_src;
         b->nsim = nsim;
         b->bytes = request_footprint(r->grid, nsim);
-        sesnt_grid_t g = r->grid;
-        g.batch = nsim;
-        int rc = sesnt_create(&g, &b->h);
-        auto ptr = [&](int q) -> const float * { return r->model[q].empty() ? nullptr : r->model[q].data(); };
-        if (!rc) rc = sesnt_set_model(b->h, ptr(0), ptr(1), ptr(2), ptr(3), ptr(4), ptr(5), ptr(6));
-        const int NP = (g.lpd + 1) * (g.lpd + 1) * (g.lpd + 1);
-        for (int s = 0; !rc && s < nsim; ++s) {
-            const int q = b->src0 + s;
-            rc = sesnt_add_source(b->h, s, r->src_elem[3 * q], r->src_elem[3 * q + 1], r->src_elem[3 * q + 2],
-                                  &r->src_vm[(size_t)q * NP], r->src_kind[q], &r->src_comp[(size_t)q * 6],
-                                  &r->src_stf[(size_t)q * g.nt], g.nt);
-        }
-        for (int k = 0; !rc && k < r->nrec; ++k) {
-            const int idx = sesnt_add_receiver(b->h, r->rec_elem[3 * k], r->rec_elem[3 * k + 1],
-                                               r->rec_elem[3 * k + 2], &r->rec_vm[(size_t)k * NP], r->rec_mask[k]);
-            if (idx < 0) rc = idx;
-        }
-        if (rc) {
-            r->failed = true;
-            r->error = b->h ? sesnt_last_error(b->h) : sesnt_last_error(nullptr);
-            if (b->h) sesnt_destroy(b->h);
-            r->done = true;
-            r->t_done = Clock::now();
-            ++failed;
-            it = queue.erase(it);
-            cv_done.notify_all();
-            continue;
-        }
-        cudaEventCreateWithFlags(&b->ev, cudaEventDisableTiming);
         used_bytes += b->bytes;
         if (!r->started) {
             r->started = true;
@@ -154,6 +133,8 @@ bool sesnt_server::admit_locked() {
         }
         r->next_src += nsim;
         if (r->next_src >= r->nsrc) it = queue.erase(it);
+        setup_queue.push_back(b.get());
+        cv_setup.notify_one();
         active.push_back(std::move(b));
         any_started = true;
     }
@@ -176,12 +157,25 @@ void sesnt_server::finish_batch(Batch *b) {
     b->h = nullptr;
     used_bytes -= b->bytes;
     r->batches_done++;
-    if (r->next_src >= r->nsrc) {
-        // all sources have been handed to batches; done when none is active
+    request_settled_locked(r, b);
+}
+
+void sesnt_server::remove_active_locked(const Batch *b) {
+    for (size_t q = 0; q < active.size(); ++q)
+        if (active[q].get() == b) {
+            active.erase(active.begin() + q);
+            return;
+        }
+}
+
+// A batch of r is gone (finished or failed): r is done when all its sources
+// have been handed to batches (or it failed) and none is left.
+void sesnt_server::request_settled_locked(Request *r, const Batch *gone) {
+    if (r->next_src >= r->nsrc || r->failed) {
         bool pending = false;
         for (auto &x : active)
-            if (x.get() != b && x->req == r) pending = true;
-        if (!pending) {
+            if (x.get() != gone && x->req == r) pending = true;
+        if (!pending && !r->done) {
             r->done = true;
             r->t_done = Clock::now();
             if (r->failed) {
@@ -200,6 +194,56 @@ void sesnt_server::finish_batch(Batch *b) {
     }
 }
 
+// Creates and loads the handles of admitted batches, outside the scheduler.
+void sesnt_server::run_setup() {
+    cudaSetDevice(device);
+    for (;;) {
+        Batch *b = nullptr;
+        {
+            std::unique_lock<std::mutex> lk(mu);
+            cv_setup.wait(lk, [&] { return stop.load() || !setup_queue.empty(); });
+            if (stop.load()) return;
+            b = setup_queue.front();
+            setup_queue.pop_front();
+        }
+        Request *r = b->req;
+        sesnt_grid_t g = r->grid;
+        g.batch = b->nsim;
+        sesnt_t *h = nullptr;
+        int rc = sesnt_create(&g, &h);
+        auto ptr = [&](int q) -> const float * { return r->model[q].empty() ? nullptr : r->model[q].data(); };
+        if (!rc) rc = sesnt_set_model(h, ptr(0), ptr(1), ptr(2), ptr(3), ptr(4), ptr(5), ptr(6));
+        const int NP = (g.lpd + 1) * (g.lpd + 1) * (g.lpd + 1);
+        for (int s = 0; !rc && s < b->nsim; ++s) {
+            const int q = b->src0 + s;
+            rc = sesnt_add_source(h, s, r->src_elem[3 * q], r->src_elem[3 * q + 1], r->src_elem[3 * q + 2],
+                                  &r->src_vm[(size_t)q * NP], r->src_kind[q], &r->src_comp[(size_t)q * 6],
+                                  &r->src_stf[(size_t)q * g.nt], g.nt);
+        }
+        for (int k = 0; !rc && k < r->nrec; ++k) {
+            const int idx = sesnt_add_receiver(h, r->rec_elem[3 * k], r->rec_elem[3 * k + 1], r->rec_elem[3 * k + 2],
+                                               &r->rec_vm[(size_t)k * NP], r->rec_mask[k]);
+            if (idx < 0) rc = idx;
+        }
+        cudaEvent_t ev = nullptr;
+        if (!rc && cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) rc = SESNT_ECUDA;
+        std::lock_guard<std::mutex> lk(mu);
+        if (rc) {
+            if (!r->failed) r->error = h ? sesnt_last_error(h) : sesnt_last_error(nullptr);
+            r->failed = true;
+            if (h) sesnt_destroy(h);
+            used_bytes -= b->bytes;
+            request_settled_locked(r, b);
+            remove_active_locked(b);
+        } else {
+            b->h = h;
+            b->ev = ev;
+            b->ready = true;
+        }
+        cv_work.notify_all();
+    }
+}
+
 void sesnt_server::run() {
     cudaSetDevice(device);
     auto busy_since = Clock::now();
@@ -211,7 +255,7 @@ void sesnt_server::run() {
             admit_locked();
             // launch the next chunk of every idle batch
             for (auto &b : active) {
-                if (b->in_flight) continue;
+                if (b->in_flight || !b->ready) continue;
                 const int nt = b->req->grid.nt;
                 const int n = std::min(cfg.chunk_steps, nt - b->it + 1);
                 int rc = sesnt_run(b->h, b->it, n);
@@ -250,25 +294,11 @@ void sesnt_server::run() {
             std::lock_guard<std::mutex> lk(mu);
             for (Batch *b : finished) {
                 finish_batch(b);
-                for (size_t q = 0; q < active.size(); ++q)
-                    if (active[q].get() == b) {
-                        active.erase(active.begin() + q);
-                        break;
-                    }
+                remove_active_locked(b);
             }
         }
         if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(50));
     }
-    // drain: wait for in-flight work, free handles
-    std::lock_guard<std::mutex> lk(mu);
-    for (auto &b : active) {
-        if (b->h) {
-            sesnt_synchronize(b->h);
-            sesnt_destroy(b->h);
-        }
-        if (b->ev) cudaEventDestroy(b->ev);
-    }
-    active.clear();
 }
 
 extern "C" {
@@ -290,15 +320,30 @@ int sesnt_server_create(const sesnt_server_config_t *cfg, sesnt_server_t **out) 
     }
     sesnt_server *p = s.get();
     s->worker = std::thread([p] { p->run(); });
+    s->setup = std::thread([p] { p->run_setup(); });
     *out = s.release();
     return SESNT_OK;
 }
 
 int sesnt_server_destroy(sesnt_server_t *s) {
     if (!s) return SESNT_OK;
-    s->stop.store(true);
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop.store(true);
+    }
     s->cv_work.notify_all();
+    s->cv_setup.notify_all();
+    if (s->setup.joinable()) s->setup.join();
     if (s->worker.joinable()) s->worker.join();
+    // drain: wait for in-flight work, free handles
+    for (auto &b : s->active) {
+        if (b->h) {
+            sesnt_synchronize(b->h);
+            sesnt_destroy(b->h);
+        }
+        if (b->ev) cudaEventDestroy(b->ev);
+    }
+    s->active.clear();
     delete s;
     return SESNT_OK;
 }

@@ -23,6 +23,7 @@
 
 using namespace sesnt;
 
+
 namespace sesnt {
 template <>
 const LpdOps<float> *lpd_ops<float>(int lpd) {
@@ -256,7 +257,7 @@ struct sesnt_handle {
         cudaError_t e = cudaMalloc(&p, bytes);
         if (e != cudaSuccess) {
             cudaGetLastError();
-            return fail(SESNT_ENOMEM, "cudaMalloc of %zu bytes for %s failed: %s", bytes, what,
+            return fail(SESNT_ENOMEM, "allocation of %zu bytes for %s failed: %s", bytes, what,
                         cudaGetErrorString(e));
         }
         bufs.push_back({p, bytes});
@@ -269,11 +270,12 @@ struct sesnt_handle {
         for (size_t i = 0; i < bufs.size(); ++i)
             if (bufs[i].p == p) {
                 dev_bytes -= bufs[i].n;
-                cudaFree(p);
+                free_buffer(p);
                 bufs.erase(bufs.begin() + i);
                 return;
             }
     }
+    void free_buffer(void *p) { cudaFree(p); }
     void clear_marks() {
         for (int &m : mark_it) m = -1;
     }
@@ -291,7 +293,7 @@ struct sesnt_handle {
         drop_graph();
         if (stream) cudaStreamSynchronize(stream);
         writer.reset();  // writes what is queued, then joins
-        for (auto &b : bufs) cudaFree(b.p);
+        for (auto &b : bufs) free_buffer(b.p);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
         for (cudaEvent_t ev : {ev_fork, ev_src, ev_node, ev_join})
@@ -1152,6 +1154,7 @@ int sesnt_create(const sesnt_grid_t *grid, sesnt_t **out) {
     h->kahan = (grid->flags & SESNT_FLAG_KAHAN) != 0;
     h->use_graph = (grid->flags & SESNT_FLAG_NO_GRAPH) == 0;
     h->launches_per_step = 4;
+    cudaGetDevice(&h->device);
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -1209,7 +1212,6 @@ int sesnt_create(const sesnt_grid_t *grid, sesnt_t **out) {
         g_create_error = h->err;
         return rc;
     }
-    cudaGetDevice(&h->device);
     if ((h->dbl ? lpd_ops<double>(h->N)->prepare() : lpd_ops<float>(h->N)->prepare()) != 0) {
         g_create_error = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(cudaGetLastError());
         return SESNT_ECUDA;

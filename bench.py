@@ -81,6 +81,14 @@ def reduce(x, op):
     return float(t.item())
 
 
+def aggregate(units, ms):
+    """Whole-job rate of the replicas: the units all ranks processed over the
+    slowest rank's time. Returns (units/s, slowest ms)."""
+    ms_max = reduce(ms, "max")
+    total = reduce(units, "sum")
+    return total / (ms_max / 1e3), ms_max
+
+
 # ---------------------------------------------------------------------------
 # clocks during the timed region
 # ---------------------------------------------------------------------------
@@ -238,10 +246,7 @@ def run_ours(args):
     ms = sim.run_timed(W + 1, K)
     clk = clocks.stop()
     barrier()
-    ms_max = reduce(ms, "max")
-    units = float(g.n_loc) * K * S
-    total_units = reduce(units, "sum")
-    value = total_units / (ms_max / 1e3)
+    value, ms_max = aggregate(float(g.n_loc) * K * S, ms)
 
     # per-kernel event timing of the same step sequence (dominant kernel)
     prof = sim.run_profiled(W + K + 1, KP) if KP > 0 else None

@@ -308,9 +308,9 @@ int sesnt_assemble_field(sesnt_t *h, float *field);
 
 /* No counterpart in the reference. The same assembly as
  * sesnt_assemble_field, for callers that cannot allocate device memory at the
- * time of the call (a stream being captured into a CUDA graph, a time loop
- * that must not synchronise the device as cudaMalloc/cudaFree do, a host
- * that reserved all device memory up front). d_in and d_out are device
+ * time of the call (a time loop that must not synchronise the whole device
+ * as cudaMalloc/cudaFree may, a host that reserved all device memory up
+ * front). d_in and d_out are device
  * pointers to float32 fields in the reference raw layout and may be the same
  * buffer. Nothing is allocated: the unique-point sums use a fixed device
  * array of 4,194,304 floats (16 MiB) that every GPU loading this library

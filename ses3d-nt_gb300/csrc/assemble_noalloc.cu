@@ -1,8 +1,8 @@
 // sesnt_assemble_field_noalloc: assembly of shared GLL points without any
 // device allocation, for callers that cannot call cudaMalloc at that point:
-// code running while a stream is being captured into a CUDA graph, a Fortran
-// time loop that must not synchronise the device (cudaMalloc/cudaFree do),
-// or a host that sized and reserved all device memory up front.
+// a Fortran time loop that must not synchronise the whole device (as
+// cudaMalloc/cudaFree may), or a host program that sized and reserved all
+// device memory up front and has nothing left to allocate from.
 //
 // The unique-point accumulator lives in a file-scope device array of fixed
 // size (kNoAllocMaxUnique floats, 16 MiB). Every GPU that loads this library

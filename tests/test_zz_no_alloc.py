@@ -1,7 +1,7 @@
 """sesnt_assemble_field_noalloc, the assembly entry point for callers that
-cannot allocate device memory when they call it (for example while a stream
-is being captured into a CUDA graph, or inside a time loop that must not
-synchronise the device the way cudaMalloc/cudaFree do). It must give the same
+cannot allocate device memory when they call it (for example inside a time
+loop that must not synchronise the whole device the way cudaMalloc/cudaFree
+may, or in a program that reserved all device memory up front). It must give the same
 sums as the allocating sesnt_assemble_field, call after call, although every
 call reuses one fixed device array.
 

@@ -57,6 +57,8 @@ extern "C" {
 #define SESNT_FLAG_STRAIN 32u     /* keep the displacement gradient (src/evolution.f90:179-187):
                                      9 more element-local fields read and written each step;
                                      enables SESNT_FIELD_EXX .. _EZZ */
+#define SESNT_FLAG_NO_PAIR 128u   /* batched elastic steps: one simulation per thread instead of two
+                                     (same results up to the order of the atomic adds) */
 #define SESNT_FLAG_ROTATION 64u   /* compute the rotation strain of the whole volume every step;
                                      enables SESNT_FIELD_ROT_* after any step (without it they
                                      are available after the steps of a rotation snapshot) */

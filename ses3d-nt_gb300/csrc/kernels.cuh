@@ -51,6 +51,10 @@ namespace sesnt {
 #ifndef SESNT_MINB_384
 #define SESNT_MINB_384 3
 #endif
+// Resident blocks the paired-simulation elastic kernel is sized for (FP32).
+#ifndef SESNT_MINB_PAIR
+#define SESNT_MINB_PAIR 6
+#endif
 
 template <int N>
 struct ElemCfg {
@@ -62,6 +66,8 @@ struct ElemCfg {
     // resident blocks per SM the register allocation is sized for
     static constexpr int MINB = NT <= 128 ? 2 * SESNT_MINB_256
                               : (NT <= 256 ? SESNT_MINB_256 : (NT <= 384 ? SESNT_MINB_384 : (NT <= 512 ? 2 : 1)));
+    // the same for the paired-simulation elastic kernel (two points' state per thread)
+    static constexpr int MINB_PAIR = NT <= 128 ? SESNT_MINB_PAIR : (NT <= 256 ? 3 : (NT <= 384 ? 2 : 1));
 };
 
 // Bounds-check builds (-DSESNT_BOUNDS_CHECK): a global index outside its
@@ -179,38 +185,17 @@ __device__ __forceinline__ void complete_gradient(const StepArgs<T> &a, const T 
     g[kDuZX] = ezx; g[kDuYZ] = eyz; g[kDuZY] = ezy;
 }
 
-// The rest of one element-local point's step, from its raw velocity gradient
-// e[9] (layout of strain_contract) and velocity. DU: integrate this point's
-// displacement gradient `du` (stride nloc); a compile-time switch, since even
-// a skipped branch measured 1.5% on the step. SMEM: sig/mem point into shared
-// memory (plain stores instead of streaming global stores).
-template <int N, typename T, int NSLS, bool ANISO, bool DU = false, bool SMEM = false>
-__device__ __forceinline__ void point_update(const StepArgs<T> &a, const T (&e)[9], T vx, T vy, T vz, int p, int i,
-                                             int j, int k, int ex, int ey, int ez, T lam, T mu, T tau, T cA, T cB,
-                                             T cC, const T (&sg)[6], const T (&m)[6][NSLS > 0 ? NSLS : 1], T *sig,
-                                             T *mem, size_t cs, size_t nloc, T *my, T *du) {
-    constexpr int P = N + 1, NP = P * P * P;
-    T g[9];
-    complete_gradient<N, T>(a, e, vx, vy, vz, i, k, ex, ez, g);
-    T exx = g[kDuXX], eyy = g[kDuYY], ezz = g[kDuZZ], exy = g[kDuXY], eyx = g[kDuYX], exz = g[kDuXZ],
-      ezx = g[kDuZX], eyz = g[kDuYZ], ezy = g[kDuZY];
-    const T rr = a.r[ez * P + k];
-    const T rs = rr * a.sin_t[ex * P + i];
-    if constexpr (DU) {
-        // displacement gradient du += dt * (completed velocity gradient)
-        // before the symmetrisation (src/evolution.f90:179-187)
-#pragma unroll
-        for (int c = 0; c < 9; ++c) du[c * nloc] = du[c * nloc] + a.dt * g[c];
-    }
-    exy = (exy + eyx) * T(0.5);
-    exz = (exz + ezx) * T(0.5);
-    eyz = (eyz + ezy) * T(0.5);
-
-    // stress rates
+// Stress rates from the symmetrised strain rates (src/evolution.f90:287-296),
+// or the standard-linear-solid form with the memory variables m
+// (:216-284, the commented branch, with the Mxy/Mxz/Myz sums fixed), plus
+// the anisotropic A, B, C terms.
+template <typename T, int NSLS, bool ANISO>
+__device__ __forceinline__ void stress_rates(T exx, T eyy, T ezz, T exy, T exz, T eyz, T lam, T mu, T tau, T cA,
+                                             T cB, T cC, const T (&m)[6][NSLS > 0 ? NSLS : 1], T &rxx, T &ryy,
+                                             T &rzz, T &rxy, T &rxz, T &ryz) {
     const T third = T(1) / T(3);
     const T two_mu = T(2) * mu;
     const T tr = exx + eyy + ezz;
-    T rxx, ryy, rzz, rxy, rxz, ryz;
     if constexpr (NSLS > 0) {
         const T mu_tau = (T(1) + tau) * mu;
         const T kappa = lam + two_mu * third;
@@ -246,6 +231,38 @@ __device__ __forceinline__ void point_update(const StepArgs<T> &a, const T (&e)[
         rxz += T(2) * cB * exz;
         ryz += T(2) * cB * eyz;
     }
+}
+
+// The rest of one element-local point's step, from its raw velocity gradient
+// e[9] (layout of strain_contract) and velocity. DU: integrate this point's
+// displacement gradient `du` (stride nloc); a compile-time switch, since even
+// a skipped branch measured 1.5% on the step. SMEM: sig/mem point into shared
+// memory (plain stores instead of streaming global stores).
+template <int N, typename T, int NSLS, bool ANISO, bool DU = false, bool SMEM = false>
+__device__ __forceinline__ void point_update(const StepArgs<T> &a, const T (&e)[9], T vx, T vy, T vz, int p, int i,
+                                             int j, int k, int ex, int ey, int ez, T lam, T mu, T tau, T cA, T cB,
+                                             T cC, const T (&sg)[6], const T (&m)[6][NSLS > 0 ? NSLS : 1], T *sig,
+                                             T *mem, size_t cs, size_t nloc, T *my, T *du) {
+    constexpr int P = N + 1, NP = P * P * P;
+    T g[9];
+    complete_gradient<N, T>(a, e, vx, vy, vz, i, k, ex, ez, g);
+    T exx = g[kDuXX], eyy = g[kDuYY], ezz = g[kDuZZ], exy = g[kDuXY], eyx = g[kDuYX], exz = g[kDuXZ],
+      ezx = g[kDuZX], eyz = g[kDuYZ], ezy = g[kDuZY];
+    const T rr = a.r[ez * P + k];
+    const T rs = rr * a.sin_t[ex * P + i];
+    if constexpr (DU) {
+        // displacement gradient du += dt * (completed velocity gradient)
+        // before the symmetrisation (src/evolution.f90:179-187)
+#pragma unroll
+        for (int c = 0; c < 9; ++c) du[c * nloc] = du[c * nloc] + a.dt * g[c];
+    }
+    exy = (exy + eyx) * T(0.5);
+    exz = (exz + ezx) * T(0.5);
+    eyz = (eyz + ezy) * T(0.5);
+
+    T rxx, ryy, rzz, rxy, rxz, ryz;
+    stress_rates<T, NSLS, ANISO>(exx, eyy, ezz, exy, exz, eyz, lam, mu, tau, cA, cB, cC, m, rxx, ryy, rzz, rxy, rxz,
+                                 ryz);
     // integrate, taper the stored stress
     const T sxx = sg[0] + a.dt * rxx;
     const T sxy = sg[1] + a.dt * rxy;
@@ -410,6 +427,171 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::M
         atomicAdd(F + u, fx);
         atomicAdd(F + nuni + u, fy);
         atomicAdd(F + 2 * nuni + u, fz);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Batched elastic step with two simulations per thread (k_element_pair): the
+// same element point of simulations s0 and s0+1 of the batch. The two share
+// every derivative-table load of the line contractions, the metric, taper
+// and quadrature factors, the material and the index arithmetic, which the
+// batched elastic step is bound by (load/store and issue, not HBM). The
+// per-simulation arithmetic and its order are those of k_element.
+// ---------------------------------------------------------------------------
+template <int N, typename T, bool ANISO>
+__global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::MINB_PAIR : 1) k_element_pair(const StepArgs<T> a) {
+    constexpr int P = ElemCfg<N>::P, NP = ElemCfg<N>::NP, EPB = ElemCfg<N>::EPB, NT = ElemCfg<N>::NT;
+    constexpr int NPS = state_stride(NP);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sD = reinterpret_cast<T *>(smem_raw);  // [4][P*P]
+    T *sv = sD + 4 * P * P;                   // [EPB][2][3][NP]
+    T *sf = sv + EPB * 6 * NP;                // [EPB][2][9][NP]
+
+    const int S = a.S, SP = S / 2;
+    const int s0 = 2 * (blockIdx.x % SP);
+    const int g = blockIdx.x / SP;
+    const int t = threadIdx.x;
+    for (int x = t; x < 4 * P * P; x += NT) sD[x] = a.tabD[x];
+
+    const int le = t / NP;
+    const int p = t - le * NP;
+    const int e = g * EPB + le;
+    bool act = (le < EPB) && (e < a.nel);
+    const int i = p % P, j = (p / P) % P, k = p / (P * P);
+    const size_t nuni = (size_t)a.nuni, nloc = (size_t)a.nloc;
+    const size_t li = (size_t)e * NP + p;
+    const size_t sb = (size_t)e * S + s0;  // simulation s0+1 follows at sb + 1
+    T *sig0 = a.sig + sb * 6 * NPS + p;
+    T *sig1 = sig0 + 6 * NPS;
+    act = act && in_range(unique_index<N>(a.NXU, a.NYU, e % a.nx, (e / a.nx) % a.ny, e / (a.nx * a.ny), i, j, k),
+                          nuni, a.err) &&
+          in_range(li, nloc, a.err) && in_range((sb + 1) * 6 * NPS + 5 * NPS + p, (size_t)a.nel * S * 6 * NPS, a.err);
+    int ex = 0, ey = 0, ez = 0;
+    size_t u = 0;
+    T lam = 0, mu = 0, cA = 0, cB = 0, cC = 0;
+    T sg0[6] = {0, 0, 0, 0, 0, 0}, sg1[6] = {0, 0, 0, 0, 0, 0};
+    T *v0 = sv + le * 6 * NP, *v1 = v0 + 3 * NP;
+    if (act) {  // every global load first, as in k_element
+        ex = e % a.nx;
+        ey = (e / a.nx) % a.ny;
+        ez = e / (a.nx * a.ny);
+        u = unique_index<N>(a.NXU, a.NYU, ex, ey, ez, i, j, k);
+        const T *va = a.v + (size_t)s0 * 3 * nuni, *vb = va + 3 * nuni;
+        const T ax = va[u], ay = va[nuni + u], az = va[2 * nuni + u];
+        const T bx = vb[u], by = vb[nuni + u], bz = vb[2 * nuni + u];
+        lam = ld_stream(a.lam + li);
+        mu = ld_stream(a.mu + li);
+        if constexpr (ANISO) {
+            cA = ld_stream(a.A + li);
+            cB = ld_stream(a.B + li);
+            cC = ld_stream(a.C + li);
+        }
+#pragma unroll
+        for (int c = 0; c < 6; ++c) {
+            sg0[c] = ld_stream(sig0 + c * NPS);
+            sg1[c] = ld_stream(sig1 + c * NPS);
+        }
+        v0[p] = ax;
+        v0[NP + p] = ay;
+        v0[2 * NP + p] = az;
+        v1[p] = bx;
+        v1[NP + p] = by;
+        v1[2 * NP + p] = bz;
+    }
+    __syncthreads();
+    if (act) {
+        // line contractions of both simulations with one set of table loads
+        T e0[9], e1[9];
+#pragma unroll
+        for (int c = 0; c < 9; ++c) e0[c] = e1[c] = 0;
+        const T *Dx = sD, *Dy = sD + P * P, *Dz = sD + 2 * P * P;
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            const int px_ = q + P * (j + P * k), py_ = i + P * (q + P * k), pz_ = i + P * (j + P * q);
+            const T dx = Dx[q * P + i], dy = Dy[q * P + j], dz = Dz[q * P + k];
+            e0[0] += v0[px_] * dx;
+            e0[1] += v0[NP + px_] * dx;
+            e0[2] += v0[2 * NP + px_] * dx;
+            e0[3] += v0[py_] * dy;
+            e0[4] += v0[NP + py_] * dy;
+            e0[5] += v0[2 * NP + py_] * dy;
+            e0[6] += v0[pz_] * dz;
+            e0[7] += v0[NP + pz_] * dz;
+            e0[8] += v0[2 * NP + pz_] * dz;
+            e1[0] += v1[px_] * dx;
+            e1[1] += v1[NP + px_] * dx;
+            e1[2] += v1[2 * NP + px_] * dx;
+            e1[3] += v1[py_] * dy;
+            e1[4] += v1[NP + py_] * dy;
+            e1[5] += v1[2 * NP + py_] * dy;
+            e1[6] += v1[pz_] * dz;
+            e1[7] += v1[NP + pz_] * dz;
+            e1[8] += v1[2 * NP + pz_] * dz;
+        }
+        T g0[9], g1[9];
+        complete_gradient<N, T>(a, e0, v0[p], v0[NP + p], v0[2 * NP + p], i, k, ex, ez, g0);
+        complete_gradient<N, T>(a, e1, v1[p], v1[NP + p], v1[2 * NP + p], i, k, ex, ez, g1);
+        const T tp = taper_value(a.px[ex * P + i], a.py[ey * P + j], a.pz[ez * P + k], a.inv_alpha);
+        const T rr = a.r[ez * P + k];
+        const T rs = rr * a.sin_t[ex * P + i];
+        const T W = a.w[i] * a.w[j] * a.w[k];
+        const T gx = W * rs * a.c1, gy = W * rr * a.c2, gz = W * (rr * rs) * a.c3;
+        const T m[6][1] = {{0}, {0}, {0}, {0}, {0}, {0}};
+        auto update = [&](const T(&gg)[9], const T(&sg)[6], T *sig, T *my) {
+            const T exx = gg[kDuXX], eyy = gg[kDuYY], ezz = gg[kDuZZ];
+            const T exy = (gg[kDuXY] + gg[kDuYX]) * T(0.5);
+            const T exz = (gg[kDuXZ] + gg[kDuZX]) * T(0.5);
+            const T eyz = (gg[kDuYZ] + gg[kDuZY]) * T(0.5);
+            T rxx, ryy, rzz, rxy, rxz, ryz;
+            stress_rates<T, 0, ANISO>(exx, eyy, ezz, exy, exz, eyz, lam, mu, T(0), cA, cB, cC, m, rxx, ryy, rzz, rxy,
+                                      rxz, ryz);
+            const T sxx = sg[0] + a.dt * rxx;
+            const T sxy = sg[1] + a.dt * rxy;
+            const T sxz = sg[2] + a.dt * rxz;
+            const T syy = sg[3] + a.dt * ryy;
+            const T syz = sg[4] + a.dt * ryz;
+            const T szz = sg[5] + a.dt * rzz;
+            st_stream(sig, sxx * tp);
+            st_stream(sig + NPS, sxy * tp);
+            st_stream(sig + 2 * NPS, sxz * tp);
+            st_stream(sig + 3 * NPS, syy * tp);
+            st_stream(sig + 4 * NPS, syz * tp);
+            st_stream(sig + 5 * NPS, szz * tp);
+            my[0 * NP + p] = sxx * gx;
+            my[1 * NP + p] = sxy * gy;
+            my[2 * NP + p] = sxz * gz;
+            my[3 * NP + p] = sxy * gx;
+            my[4 * NP + p] = syy * gy;
+            my[5 * NP + p] = syz * gz;
+            my[6 * NP + p] = sxz * gx;
+            my[7 * NP + p] = syz * gy;
+            my[8 * NP + p] = szz * gz;
+        };
+        update(g0, sg0, sig0, sf + le * 18 * NP);
+        update(g1, sg1, sig1, sf + le * 18 * NP + 9 * NP);
+    }
+    __syncthreads();
+    if (act) {
+        const T *f0 = sf + le * 18 * NP, *f1 = f0 + 9 * NP, *Dt = sD + 3 * P * P;
+        T ax = 0, ay = 0, az = 0, bx = 0, by = 0, bz = 0;
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            const int px_ = q + P * (j + P * k), py_ = i + P * (q + P * k), pz_ = i + P * (j + P * q);
+            const T di = Dt[i * P + q], dj = Dt[j * P + q], dk = Dt[k * P + q];
+            ax += f0[2 * NP + pz_] * dk + f0[1 * NP + py_] * dj + f0[0 * NP + px_] * di;
+            ay += f0[5 * NP + pz_] * dk + f0[4 * NP + py_] * dj + f0[3 * NP + px_] * di;
+            az += f0[8 * NP + pz_] * dk + f0[7 * NP + py_] * dj + f0[6 * NP + px_] * di;
+            bx += f1[2 * NP + pz_] * dk + f1[1 * NP + py_] * dj + f1[0 * NP + px_] * di;
+            by += f1[5 * NP + pz_] * dk + f1[4 * NP + py_] * dj + f1[3 * NP + px_] * di;
+            bz += f1[8 * NP + pz_] * dk + f1[7 * NP + py_] * dj + f1[6 * NP + px_] * di;
+        }
+        T *F0 = a.F + (size_t)s0 * 3 * nuni, *F1 = F0 + 3 * nuni;
+        atomicAdd(F0 + u, ax);
+        atomicAdd(F0 + nuni + u, ay);
+        atomicAdd(F0 + 2 * nuni + u, az);
+        atomicAdd(F1 + u, bx);
+        atomicAdd(F1 + nuni + u, by);
+        atomicAdd(F1 + 2 * nuni + u, bz);
     }
 }
 
@@ -677,6 +859,13 @@ template <int N, typename T, int NSLS, bool ANISO>
 int launch_element_v(const StepArgs<T> &a, void *stream) {
     using C = ElemCfg<N>;
     const long long groups = (long long)((a.nel + C::EPB - 1) / C::EPB) * a.S;
+    if constexpr (NSLS == 0) {
+        if (a.S >= 2 && a.S % 2 == 0 && !a.du && a.pair) {
+            const size_t smem2 = sizeof(T) * (4 * C::P * C::P + C::EPB * 24 * C::NP);
+            k_element_pair<N, T, ANISO><<<(unsigned)(groups / 2), C::NT, smem2, (cudaStream_t)stream>>>(a);
+            return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+        }
+    }
     const size_t smem = sizeof(T) * (4 * C::P * C::P + C::EPB * 12 * C::NP);
     if (a.du) k_element<N, T, NSLS, ANISO, true><<<(unsigned)groups, C::NT, smem, (cudaStream_t)stream>>>(a);
     else k_element<N, T, NSLS, ANISO, false><<<(unsigned)groups, C::NT, smem, (cudaStream_t)stream>>>(a);
@@ -694,6 +883,12 @@ int prepare_variant() {
     if (e == cudaSuccess && smem > 48 * 1024)
         e = cudaFuncSetAttribute(k_element<N, T, NSLS, ANISO, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem);
+    if constexpr (NSLS == 0) {
+        const size_t smem2 = sizeof(T) * (4 * C::P * C::P + C::EPB * 24 * C::NP);
+        if (e == cudaSuccess && smem2 > 48 * 1024)
+            e = cudaFuncSetAttribute(k_element_pair<N, T, ANISO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem2);
+    }
     return e == cudaSuccess ? 0 : -1;
 }
 

@@ -328,6 +328,7 @@ struct sesnt_handle {
         a.nrec = nrec_dev; a.rec_elem = d_rec_elem; a.rec_vm = (const T *)d_rec_vm; a.seis = (T *)d_seis;
         a.d_it = d_it; a.step_off = 0;
         a.persistent = (g.flags & SESNT_FLAG_PERSISTENT_ELEMENT) ? 1 : 0;
+        a.pair = (g.flags & SESNT_FLAG_NO_PAIR) ? 0 : 1;
         a.contraction = (g.flags & SESNT_FLAG_TC_TF32X3) ? 1 : ((g.flags & SESNT_FLAG_TC_BF16X3) ? 2 : 0);
         a.two_over_d[0] = (T)two_over_d[0];
         a.two_over_d[1] = (T)two_over_d[1];

@@ -79,6 +79,7 @@ struct StepArgs {
     const int *d_it;
     int step_off;
     int persistent;  // element kernel: persistent prefetching variant (1) or one block per group (0)
+    int pair;        // batched elastic steps: two simulations per thread (k_element_pair)
     int contraction; // element kernel contractions: 0 CUDA cores, 1 tensor cores TF32x3, 2 tensor cores BF16x3
     T two_over_d[3]; // 2/dx_elm, 2/dy_elm, 2/dz_elm
     int *err;        // device error word (a bounded wait ran out)

@@ -209,21 +209,24 @@ def test_anisotropy_and_single_force(gpu, sesnt_lib, oracle_mod):
         assert e < TOL
 
 
-def test_batch_matches_independent_runs(gpu, sesnt_lib, oracle_mod):
+@pytest.mark.parametrize("batch", [3, 4])
+def test_batch_matches_independent_runs(gpu, sesnt_lib, oracle_mod, batch):
+    """Batch 3 runs one simulation per thread; batch 4 (elastic, even) the
+    paired-simulation kernel."""
     wl = small_workload(4, nt=300)
     g = copy.copy(wl.grid)
-    g.batch = 3
+    g.batch = batch
     srcs = []
-    for s in range(3):
+    for s in range(batch):
         src = copy.copy(wl.sources[0])
         src.sim = s
         src.lat = 34.0 + s
         src.lon = 3.5 + 1.5 * s
         src.comp = tuple((1.0 + 0.5 * s) * c for c in src.comp)
         srcs.append(src)
-    bw = workloads.Workload("batch3", g, wl.model, srcs, wl.receivers)
+    bw = workloads.Workload("batch", g, wl.model, srcs, wl.receivers)
     gs, _, _ = run_gpu(bw, 300, fields=())
-    for s in range(3):
+    for s in range(batch):
         one = workloads.Workload("one", wl.grid, wl.model, [copy.copy(srcs[s])], wl.receivers)
         one.sources[0].sim = 0
         os_, _, _ = run_oracle(oracle_mod, one, 300)
@@ -311,6 +314,34 @@ def test_samples_read_while_later_steps_run(gpu, sesnt_lib):
             assert np.abs(seis).max() > 0
             assert np.array_equal(np.moveaxis(got, 0, -1), seis)
             sim.reset()
+
+
+def batched(wl, batch):
+    g = copy.copy(wl.grid)
+    g.batch = batch
+    srcs = []
+    for s in range(batch):
+        src = copy.copy(wl.sources[0])
+        src.sim, src.lat, src.lon = s, 33.5 + 0.8 * s, 3.0 + 1.1 * s
+        src.comp = tuple((1.0 + 0.3 * s) * c for c in src.comp)
+        srcs.append(src)
+    return workloads.Workload("batch%d" % batch, g, wl.model, srcs, wl.receivers)
+
+
+@pytest.mark.parametrize("lpd,aniso,batch", [(4, False, 2), (4, True, 4), (2, False, 2), (3, False, 4),
+                                              (5, True, 2), (6, False, 2), (7, False, 2)])
+def test_paired_batch_kernel_matches_single(gpu, sesnt_lib, lpd, aniso, batch):
+    """Batched elastic steps with two simulations per thread against one per
+    thread (SESNT_FLAG_NO_PAIR): the same step up to the order of the atomic
+    adds, in FP32 and FP64."""
+    bw = batched(small_workload(lpd, aniso=aniso, nt=150), batch)
+    for prec, tol in ((4, 1e-5), (8, 1e-12)):
+        a, fa, _ = run_gpu(with_grid(bw, precision=prec), 150, fields=("vz", "sxy"))
+        b, fb, _ = run_gpu(with_grid(bw, precision=prec, flags=sesnt.FLAG_NO_PAIR), 150, fields=("vz", "sxy"))
+        assert np.abs(a).max() > 0
+        assert rel_l2(a, b) < tol
+        for k in fa:
+            assert rel_l2(fa[k], fb[k]) < tol, k
 
 
 def test_bulk_copy_wait_runs_out_and_reports(gpu, sesnt_lib):

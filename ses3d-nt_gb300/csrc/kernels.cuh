@@ -51,9 +51,10 @@ namespace sesnt {
 #ifndef SESNT_MINB_384
 #define SESNT_MINB_384 3
 #endif
-// Resident blocks the paired-simulation elastic kernel is sized for (FP32).
+// Resident blocks the paired-simulation elastic kernel is sized for (FP32):
+// 8 (64 registers, no spills) measured 1% faster than 6 and 5% faster than 4.
 #ifndef SESNT_MINB_PAIR
-#define SESNT_MINB_PAIR 6
+#define SESNT_MINB_PAIR 8
 #endif
 
 template <int N>

@@ -288,9 +288,13 @@ def run_ours(args):
                     tr = json.load(f)
                 if tr.get("workload") == wl.name:
                     traffic = tr.get("dram_bytes_per_launch")
+                    if "tensor_pipe_active_pct" in tr:
+                        line["tensor_pipe_active_pct"] = tr["tensor_pipe_active_pct"]  # from the ncu capture
             except Exception:
                 traffic = None
-        kname = "k_element_tc" if args.element.startswith("tc_") else "k_element"
+        kname = "k_element_tc" if args.element.startswith("tc_") else (
+            "k_element_tma" if args.element == "persistent" else (
+                "k_element_pair" if g.n_sls == 0 and S >= 2 and S % 2 == 0 else "k_element"))
         line["roofline"] = {"bound": "hbm", "kernel": kname, "achieved": ach, "peak": hbm,
                             "peak_source": peak_kind, "unit": "GB/s", "frac": ach / hbm,
                             "traffic": traffic, "alg_bytes_per_launch": eb}

@@ -51,6 +51,14 @@ namespace sesnt {
 #ifndef SESNT_MINB_384
 #define SESNT_MINB_384 3
 #endif
+// Where k_element loads the SLS memory variables: with the other loads at
+// the start (0) or after the line contractions, still before any store (1).
+// -1 picks by degree: late up to degree 5, early for 6 and 7. Measured on
+// 3-SLS FP32 grids of 6-12 M points: late is 4.3/1.2/3.9/5.0% faster for
+// degrees 2/3/4/5 and 1.4/2.4% slower for 6/7; FP64 (degree 4) unchanged.
+#ifndef SESNT_LATE_MEM
+#define SESNT_LATE_MEM -1
+#endif
 // Resident blocks the paired-simulation elastic kernel is sized for (FP32):
 // 8 (64 registers, no spills) measured 1% faster than 6 and 5% faster than 4.
 #ifndef SESNT_MINB_PAIR
@@ -351,6 +359,7 @@ template <int N, typename T, int NSLS, bool ANISO, bool DU>
 __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::MINB : 1) k_element(const StepArgs<T> a) {
     constexpr int P = ElemCfg<N>::P, NP = ElemCfg<N>::NP, EPB = ElemCfg<N>::EPB, NT = ElemCfg<N>::NT;
     constexpr int MS = NSLS > 0 ? NSLS : 1;
+    constexpr bool late_mem = SESNT_LATE_MEM < 0 ? N <= 5 : SESNT_LATE_MEM != 0;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *sD = reinterpret_cast<T *>(smem_raw);  // [4][P*P]
     T *sv = sD + 4 * P * P;                   // [EPB][3][NP]
@@ -371,8 +380,10 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::M
     size_t u = 0;
     const size_t nuni = (size_t)a.nuni, nloc = (size_t)a.nloc;
     const size_t li = (size_t)e * NP + p;
-    // Every global load of the step is issued here, before any store, so the
-    // loads overlap each other and the line contractions.
+    // Every global load of the step is issued before any store, so the loads
+    // overlap each other and the line contractions: here, or for the memory
+    // variables (late_mem) right after the barrier, which leaves the
+    // scheduler fewer live registers while the velocities are staged.
     T lam = 0, mu = 0, tau = 0, cA = 0, cB = 0, cC = 0;
     T sg[6] = {0, 0, 0, 0, 0, 0};
     T m[6][MS];
@@ -401,7 +412,7 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::M
         }
 #pragma unroll
         for (int c = 0; c < 6; ++c) sg[c] = ld_stream(sig + c * NPS);
-        if constexpr (NSLS > 0) {
+        if constexpr (NSLS > 0 && !late_mem) {
             tau = ld_stream(a.tau + li);
 #pragma unroll
             for (int c = 0; c < 6; ++c)
@@ -416,6 +427,13 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::M
     __syncthreads();
     if (act) {
         const T *svx = sv + le * 3 * NP;
+        if constexpr (NSLS > 0 && late_mem) {
+            tau = ld_stream(a.tau + li);
+#pragma unroll
+            for (int c = 0; c < 6; ++c)
+#pragma unroll
+                for (int q = 0; q < NSLS; ++q) m[c][q] = ld_stream(mem + (size_t)(c * NSLS + q) * NPS);
+        }
         point_step<N, T, NSLS, ANISO, DU>(a, sD, svx, svx + NP, svx + 2 * NP, p, i, j, k, ex, ey, ez, lam, mu, tau,
                                           cA, cB, cC, sg, m, sig, mem, NPS, nloc, sf + le * 9 * NP,
                                           DU ? a.du + (size_t)s * 9 * nloc + li : nullptr);

@@ -217,6 +217,21 @@ def cpu_oracle_rate(wl, budget_s, max_steps=None, warm=2):
 # ---------------------------------------------------------------------------
 # arms
 # ---------------------------------------------------------------------------
+def element_kernel_name(element, g):
+    """The element kernel the library launches for this grid and --element
+    choice (the launch rules of kernels.cuh:launch_element)."""
+    import sesnt
+    if element.startswith("tc_"):
+        return "k_element_tc"
+    if element == "persistent":
+        return "k_element_tma"
+    if g.n_sls == 0 and g.batch >= 2 and g.batch % 2 == 0:
+        return "k_element_pair"
+    if g.n_sls > 0 and g.lpd >= 4 and element != "unstaged" and not (g.flags & sesnt.FLAG_STRAIN):
+        return "k_element_stage"
+    return "k_element"
+
+
 def run_ours(args):
     import numpy as np
 
@@ -228,7 +243,7 @@ def run_ours(args):
     wl = make_workload(args.workload, W + K + KP + 1)
     g = wl.grid
     g.flags |= {"persistent": sesnt.FLAG_PERSISTENT_ELEMENT, "tc_tf32x3": sesnt.FLAG_TC_TF32X3,
-                "tc_bf16x3": sesnt.FLAG_TC_BF16X3}.get(args.element, 0)
+                "tc_bf16x3": sesnt.FLAG_TC_BF16X3, "unstaged": sesnt.FLAG_NO_STAGE}.get(args.element, 0)
     S = g.batch
     hbm, peak_kind = peaks()
 
@@ -279,9 +294,9 @@ def run_ours(args):
         prof = [float(x) for x in prof]
         line["kernels_ms_per_step"] = {"element": prof[0] / KP, "sources": prof[1] / KP, "node": prof[2] / KP,
                                        "receivers": prof[3] / KP}
+        kname = element_kernel_name(args.element, g)
         traffic = None
-        tr_path = os.path.join(ROOT, "profiles", "%s_%s.traffic.json"
-                               % ("k_element_tc" if args.element.startswith("tc_") else "k_element", wl.name))
+        tr_path = os.path.join(ROOT, "profiles", "%s_%s.traffic.json" % (kname, wl.name))
         if os.path.exists(tr_path):
             try:
                 with open(tr_path) as f:
@@ -292,9 +307,6 @@ def run_ours(args):
                         line["tensor_pipe_active_pct"] = tr["tensor_pipe_active_pct"]  # from the ncu capture
             except Exception:
                 traffic = None
-        kname = "k_element_tc" if args.element.startswith("tc_") else (
-            "k_element_tma" if args.element == "persistent" else (
-                "k_element_pair" if g.n_sls == 0 and S >= 2 and S % 2 == 0 else "k_element"))
         line["roofline"] = {"bound": "hbm", "kernel": kname, "achieved": ach, "peak": hbm,
                             "peak_source": peak_kind, "unit": "GB/s", "frac": ach / hbm,
                             "traffic": traffic, "alg_bytes_per_launch": eb}
@@ -489,7 +501,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-seconds", type=float, default=60.0)
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
-    ap.add_argument("--element", default="simple", choices=["persistent", "simple", "tc_tf32x3", "tc_bf16x3"],
+    ap.add_argument("--element", default="simple",
+                    choices=["persistent", "simple", "unstaged", "tc_tf32x3", "tc_bf16x3"],
                     help="element kernel variant (all compute the full step; tc_*: tcgen05 contractions)")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -59,6 +59,9 @@ extern "C" {
                                      enables SESNT_FIELD_EXX .. _EZZ */
 #define SESNT_FLAG_NO_PAIR 128u   /* batched elastic steps: one simulation per thread instead of two
                                      (same results up to the order of the atomic adds) */
+#define SESNT_FLAG_NO_STAGE 256u  /* SLS steps: each thread loads its stress and memory variables
+                                     (k_element) instead of one bulk copy per element staging
+                                     them in shared memory (k_element_stage); same results */
 #define SESNT_FLAG_ROTATION 64u   /* compute the rotation strain of the whole volume every step;
                                      enables SESNT_FIELD_ROT_* after any step (without it they
                                      are available after the steps of a rotation snapshot) */

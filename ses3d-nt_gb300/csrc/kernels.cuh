@@ -930,6 +930,8 @@ int prepare_element() {
     if (prepare_element_tma<N, T, 0, false>() || prepare_element_tma<N, T, 0, true>() ||
         prepare_element_tma<N, T, kNsls, false>() || prepare_element_tma<N, T, kNsls, true>())
         return -1;
+    if constexpr (ElemCfg<N>::EPB == 1)
+        if (prepare_element_stage<N, T, kNsls, false>() || prepare_element_stage<N, T, kNsls, true>()) return -1;
     return 0;
 }
 
@@ -950,6 +952,12 @@ int launch_element(const StepArgs<T> &a, bool sls, bool aniso, void *stream) {
         const int r = launch_element_bulk<N, T>(a, sls, aniso, stream);
         if (r <= 0) return r;
     }
+    if constexpr (ElemCfg<N>::EPB == 1)
+        if (sls && a.stage && !a.du) {
+            const int r = aniso ? launch_element_stage<N, T, kNsls, true>(a, stream)
+                                : launch_element_stage<N, T, kNsls, false>(a, stream);
+            if (r <= 0) return r;
+        }
     if (sls) return aniso ? launch_element_v<N, T, kNsls, true>(a, stream) : launch_element_v<N, T, kNsls, false>(a, stream);
     return aniso ? launch_element_v<N, T, 0, true>(a, stream) : launch_element_v<N, T, 0, false>(a, stream);
 }

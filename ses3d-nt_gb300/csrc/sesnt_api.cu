@@ -240,9 +240,16 @@ struct sesnt_handle {
     }
     // After a synchronisation: the error word written by a kernel whose
     // bounded completion wait ran out (the tensor-core element kernel).
+    // Whether an element kernel of this handle has bounded device-side waits
+    // (tensor-core, persistent bulk-copy, or the staged SLS kernel of degrees
+    // 4-7), i.e. whether the error word can be set without the bounds check.
+    bool bounded_waits() const {
+        if (g.flags & (SESNT_FLAG_TC_TF32X3 | SESNT_FLAG_TC_BF16X3 | SESNT_FLAG_PERSISTENT_ELEMENT)) return true;
+        return sls && g.lpd >= 4 && !(g.flags & (SESNT_FLAG_NO_STAGE | SESNT_FLAG_STRAIN));
+    }
     int wait_status() {
 #ifndef SESNT_BOUNDS_CHECK
-        if (!(g.flags & (SESNT_FLAG_TC_TF32X3 | SESNT_FLAG_TC_BF16X3 | SESNT_FLAG_PERSISTENT_ELEMENT))) return SESNT_OK;
+        if (!bounded_waits()) return SESNT_OK;
 #endif
         int word = 0;
         cudaError_t e = cudaMemcpy(&word, d_err, sizeof(int), cudaMemcpyDeviceToHost);
@@ -329,6 +336,7 @@ struct sesnt_handle {
         a.d_it = d_it; a.step_off = 0;
         a.persistent = (g.flags & SESNT_FLAG_PERSISTENT_ELEMENT) ? 1 : 0;
         a.pair = (g.flags & SESNT_FLAG_NO_PAIR) ? 0 : 1;
+        a.stage = (g.flags & SESNT_FLAG_NO_STAGE) ? 0 : 1;
         a.contraction = (g.flags & SESNT_FLAG_TC_TF32X3) ? 1 : ((g.flags & SESNT_FLAG_TC_BF16X3) ? 2 : 0);
         a.two_over_d[0] = (T)two_over_d[0];
         a.two_over_d[1] = (T)two_over_d[1];

@@ -80,11 +80,12 @@ struct StepArgs {
     int step_off;
     int persistent;  // element kernel: persistent prefetching variant (1) or one block per group (0)
     int pair;        // batched elastic steps: two simulations per thread (k_element_pair)
+    int stage;       // SLS steps: state staged in shared memory by bulk copy (k_element_stage)
     int contraction; // element kernel contractions: 0 CUDA cores, 1 tensor cores TF32x3, 2 tensor cores BF16x3
     T two_over_d[3]; // 2/dx_elm, 2/dy_elm, 2/dz_elm
     int *err;        // device error word (a bounded wait ran out)
     int wait_polls;  // bound of every device-side completion wait (mbarrier polls)
-    int drop_completion;  // failure-detection test hook: the tensor-core kernel signals no completion
+    int drop_completion;  // failure-detection test hook: the tensor-core and bulk-copy kernels signal no completion
     // displacement gradient [S][9][nloc] (order kDu*), or null when not kept
     T *du;
     // receiver channels beyond vx, vy, vz (SESNT_CH_ROT_* , _M**, _F*):

@@ -33,6 +33,7 @@ FLAG_TC_BF16X3 = 16
 FLAG_STRAIN = 32
 FLAG_ROTATION = 64
 FLAG_NO_PAIR = 128
+FLAG_NO_STAGE = 256
 SOURCE_MT, SOURCE_SF = 0, 1
 WAVELETS = {"DELTA": 0, "RICKER": 1, "GAUSS": 2, "SIN**3": 3, "BRUNE": 4}
 CH_VX, CH_VY, CH_VZ, CH_N = 1, 2, 4, 8

@@ -4,7 +4,7 @@ of the handle's error word (no device assert, no trap), which the next
 synchronising call returns as SESNT_ERANGE. This is the stand-in for a
 memory sanitizer: the library is rebuilt with the checks, and a subprocess
 runs every kernel variant (degrees 2-7, elastic and SLS, anisotropy,
-batches, the persistent and tensor-core element kernels, strain and rotation
+batches, the staged, persistent and tensor-core element kernels, strain and rotation
 state, every receiver channel, snapshot fields) on small grids."""
 import os
 import subprocess
@@ -36,6 +36,10 @@ cases = [  # lpd, n_sls, aniso, kind, flags, batch
     (5, 0, False, sesnt.SOURCE_MT, sesnt.FLAG_KAHAN, 1),
     (6, 3, False, sesnt.SOURCE_MT, sesnt.FLAG_TC_BF16X3, 1),
     (7, 0, True, sesnt.SOURCE_MT, sesnt.FLAG_PERSISTENT_ELEMENT, 1),
+    (4, 3, False, sesnt.SOURCE_MT, 0, 1),
+    (5, 3, True, sesnt.SOURCE_SF, 0, 2),
+    (6, 3, False, sesnt.SOURCE_MT, 0, 2),
+    (7, 3, False, sesnt.SOURCE_MT, sesnt.FLAG_KAHAN, 1),
 ]
 for lpd, n_sls, aniso, kind, flags, batch in cases:
     wl = small_workload(lpd, n_sls=n_sls, aniso=aniso, kind=kind, nt=40)
@@ -77,4 +81,4 @@ def test_every_kernel_in_bounds(gpu, tmp_path):
     code = SCRIPT % (PKG, HERE, str(tmp_path))
     r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=900)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
-    assert "OK 8" in r.stdout
+    assert "OK 12" in r.stdout

@@ -365,6 +365,45 @@ def test_bulk_copy_wait_runs_out_and_reports(gpu, sesnt_lib):
     assert rel_l2(again, fresh) < 1e-6
 
 
+@pytest.mark.parametrize("lpd,aniso,batch", [(4, False, 1), (4, True, 3), (5, False, 2), (6, True, 1),
+                                              (6, False, 2), (7, False, 1)])
+def test_staged_kernel_matches_unstaged(gpu, sesnt_lib, lpd, aniso, batch):
+    """SLS steps with each element's stress and memory variables staged in
+    shared memory by bulk copy (k_element_stage: bulk stores for degrees 4, 5
+    and 7, register stores for 6) against per-thread loads and stores
+    (SESNT_FLAG_NO_STAGE, k_element): the same step up to the order of the
+    atomic adds, in FP32 and FP64."""
+    wl = small_workload(lpd, n_sls=3, aniso=aniso, nt=150)
+    w = batched(wl, batch) if batch > 1 else wl
+    for prec, tol in ((4, 1e-5), (8, 1e-12)):
+        a, fa, _ = run_gpu(with_grid(w, precision=prec), 150, fields=("vz", "sxy", "szz"))
+        b, fb, _ = run_gpu(with_grid(w, precision=prec, flags=sesnt.FLAG_NO_STAGE), 150, fields=("vz", "sxy", "szz"))
+        assert np.abs(a).max() > 0
+        assert rel_l2(a, b) < tol
+        for k in fa:
+            assert rel_l2(fa[k], fb[k]) < tol, k
+
+
+def test_staged_state_wait_runs_out_and_reports(gpu, sesnt_lib):
+    """The staged SLS kernel's one mbarrier wait per block is bounded: with
+    the bulk loads dropped it runs out, synchronising returns SESNT_ETIMEOUT,
+    and after sesnt_reset the handle steps normally again."""
+    wl = small_workload(4, n_sls=3, nt=40)
+    with sesnt.Simulation(wl.grid) as sim:
+        workloads.setup(sim, wl)
+        sim.set_wait_limit(64, drop_completion=True)
+        sim.run(1, 2)
+        with pytest.raises(sesnt.SesntError) as e:
+            sim.synchronize()
+        assert e.value.code == sesnt.ETIMEOUT
+        sim.set_wait_limit(1 << 22)
+        sim.reset()
+        sim.run(1, 40)
+        again = sim.seismograms()
+    fresh, _, _ = run_gpu(wl, 40, fields=())
+    assert rel_l2(again, fresh) < 1e-6
+
+
 def test_kahan_update(gpu, sesnt_lib, oracle_mod):
     wl = small_workload(4, nt=300)
     k, _, _ = run_gpu(with_grid(wl, flags=sesnt.FLAG_KAHAN), 300)

@@ -93,6 +93,32 @@ __global__ void k_import(const float *__restrict__ in, T *__restrict__ out, int 
     }
 }
 
+// Model checks on a raw host array staged on the device, before anything of
+// the handle changes. res[0]: smallest index that fails the check (mode 0:
+// not positive or not finite, rhoinv; mode 1: not finite, lambda and mu), or
+// ~0; res[1]: 1 if any value differs from `other` (mode 2: q differs from
+// FLT_MAX, i.e. attenuation is on; mode 3: a nonzero anisotropy term).
+constexpr int kCheckBlocks = 4 * 152;  // grid-stride blocks of k_check_model
+__global__ void k_check_model(const float *__restrict__ x, long long n, int mode, float other,
+                              unsigned long long *res) {
+    bool any = false;
+    unsigned long long first = ~0ull;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float v = x[i];
+        if (mode <= 1) {
+            const bool ok = isfinite(v) && (mode == 1 || v > 0.0f);
+            if (!ok && (unsigned long long)i < first) first = (unsigned long long)i;
+        } else if (v != other) {
+            any = true;
+        }
+    }
+    if (mode <= 1) {
+        if (first != ~0ull) atomicMin(res, first);
+    } else if (__any_sync(0xffffffffu, any) && (threadIdx.x & 31) == 0) {
+        atomicOr(res + 1, 1ull);
+    }
+}
+
 // tau = 6.0814 * q^-1.015 (src/model_paras.F90:407), evaluated in FP64.
 template <typename T>
 __global__ void k_tau(const T *q, T *tau, long long n) {
@@ -966,40 +992,73 @@ template <typename T>
 int set_model_impl(sesnt_t *h, const float *rhoinv, const float *lambda, const float *mu, const float *a,
                    const float *b, const float *c, const float *q) {
     const size_t nloc = (size_t)h->nloc;
+    int rc;
+    void *stage = nullptr, *checks = nullptr;
+    if ((rc = h->alloc(&stage, nloc * sizeof(float), "model staging"))) return rc;
+    // Checks pass: every host array through the staging buffer, checked on
+    // the device; the handle is left as it was if the model is rejected.
+    // [array][first bad index, any different]: rhoinv, lambda, mu, q, a, b, c
+    const float *arrays[7] = {rhoinv, lambda, mu, q, a, b, c};
+    const int modes[7] = {0, 1, 1, 2, 3, 3, 3};
+    const float others[7] = {0.0f, 0.0f, 0.0f, std::numeric_limits<float>::max(), 0.0f, 0.0f, 0.0f};
+    if ((rc = h->alloc(&checks, 7 * 2 * sizeof(unsigned long long), "model checks"))) {
+        h->release(stage);
+        return rc;
+    }
+    unsigned long long res[7][2];
+    {
+        cudaError_t e = cudaSuccess;
+        for (int x = 0; x < 7; ++x) {
+            res[x][0] = ~0ull;
+            res[x][1] = 0;
+        }
+        e = cudaMemcpyAsync(checks, res, sizeof(res), cudaMemcpyHostToDevice, h->stream);
+        for (int x = 0; x < 7 && e == cudaSuccess; ++x) {
+            if (!arrays[x]) continue;
+            e = cudaMemcpyAsync(stage, arrays[x], nloc * sizeof(float), cudaMemcpyHostToDevice, h->stream);
+            if (e == cudaSuccess) {
+                k_check_model<<<kCheckBlocks, 256, 0, h->stream>>>((const float *)stage, (long long)nloc, modes[x],
+                                                                    others[x], (unsigned long long *)checks + 2 * x);
+                e = cudaGetLastError();
+            }
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(res, checks, sizeof(res), cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        h->release(checks);
+        if (e != cudaSuccess) {
+            h->release(stage);
+            return h->cuda_fail(e, "checking model");
+        }
+    }
     // attenuation and anisotropy switches (src/evolution.f90:64-74)
-    bool has_q = false;
-    if (q)
-        for (size_t i = 0; i < nloc; ++i)
-            if (q[i] != std::numeric_limits<float>::max()) { has_q = true; break; }
-    if (has_q && !h->sls)
-        return h->fail(SESNT_EINVAL, "model has attenuation (q) but the handle was created with n_sls=0");
-    if (h->sls && !has_q) return h->fail(SESNT_EINVAL, "n_sls=3 needs a q model");
-    for (size_t i = 0; i < nloc; ++i)
-        if (!(rhoinv[i] > 0.0f) || !std::isfinite(rhoinv[i]) || !std::isfinite(lambda[i]) || !std::isfinite(mu[i]))
-            return h->fail(SESNT_EINVAL, "rhoinv must be positive and lambda, mu finite (first bad point %zu)", i);
-    bool aniso = false;
-    for (const float *x : {a, b, c})
-        if (x)
-            for (size_t i = 0; i < nloc && !aniso; ++i)
-                if (x[i] != 0.0f) aniso = true;
+    const bool has_q = q && res[3][1] != 0;
+    const bool aniso = res[4][1] || res[5][1] || res[6][1];
+    const unsigned long long bad = std::min(res[0][0], std::min(res[1][0], res[2][0]));
+    const char *why = nullptr;
+    if (has_q && !h->sls) why = "model has attenuation (q) but the handle was created with n_sls=0";
+    else if (h->sls && !has_q) why = "n_sls=3 needs a q model";
+    if (why || bad != ~0ull) {
+        h->release(stage);
+        if (why) return h->fail(SESNT_EINVAL, "%s", why);
+        return h->fail(SESNT_EINVAL, "rhoinv must be positive and lambda, mu finite (first bad point %llu)", bad);
+    }
     h->drop_graph();
     // (re)allocate the optional model arrays
-    int rc;
     if (aniso && !h->A) {
         if ((rc = h->alloc(&h->A, nloc * sizeof(T), "A"))) return rc;
         if ((rc = h->alloc(&h->B, nloc * sizeof(T), "B"))) return rc;
         if ((rc = h->alloc(&h->C, nloc * sizeof(T), "C"))) return rc;
     }
     h->aniso = aniso;
-    void *stage = nullptr, *rho_loc = nullptr;
-    if ((rc = h->alloc(&stage, nloc * sizeof(float), "model staging"))) return rc;
+    void *rho_loc = nullptr;
     if ((rc = h->alloc(&rho_loc, nloc * sizeof(T), "rhoinv"))) { h->release(stage); return rc; }
     dim3 tb(32, 8), tg((unsigned)((h->nel + 31) / 32), (unsigned)((h->NP + 31) / 32));
     auto import = [&](const float *src, void *dst) -> int {
-        cudaError_t e = cudaMemcpy(stage, src, nloc * sizeof(float), cudaMemcpyHostToDevice);
+        // stream-ordered: the copy waits for the previous import's reads of the staging buffer
+        cudaError_t e = cudaMemcpyAsync(stage, src, nloc * sizeof(float), cudaMemcpyHostToDevice, h->stream);
         if (e != cudaSuccess) return h->cuda_fail(e, "copying model");
         k_import<T><<<tg, tb, 0, h->stream>>>((const float *)stage, (T *)dst, h->NP, h->nel);
-        e = cudaStreamSynchronize(h->stream);
+        e = cudaGetLastError();
         return e == cudaSuccess ? SESNT_OK : h->cuda_fail(e, "importing model");
     };
     rc = import(rhoinv, rho_loc);
@@ -1008,7 +1067,7 @@ int set_model_impl(sesnt_t *h, const float *rhoinv, const float *lambda, const f
     if (!rc && aniso) {
         auto imp_or_zero = [&](const float *x, void *dst) -> int {
             if (x) return import(x, dst);
-            cudaError_t e = cudaMemset(dst, 0, nloc * sizeof(T));
+            cudaError_t e = cudaMemsetAsync(dst, 0, nloc * sizeof(T), h->stream);
             return e == cudaSuccess ? SESNT_OK : h->cuda_fail(e, "zeroing anisotropy");
         };
         rc = imp_or_zero(a, h->A);

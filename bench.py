@@ -151,18 +151,23 @@ class Clocks:
 # ---------------------------------------------------------------------------
 # workloads
 # ---------------------------------------------------------------------------
-def make_workload(name, nt_needed):
+def make_workload(name, nt_needed, grid=None):
+    """The named workload; `grid` = (nx, ny, nz) scales configs 2-4 down to a
+    small case of the same generator and kernels (ncu captures)."""
     import workloads
+    size = dict(zip(("nx", "ny", "nz"), grid)) if grid else {}
+    if grid and name not in ("config2", "config3", "config4", "config4_plain"):
+        raise SystemExit("--grid applies to config2, config3, config4 and config4_plain")
     if name == "config2":
-        wl = workloads.config2(nt=6000)
+        wl = workloads.config2(nt=6000, **size)
     elif name == "config1":
         wl = workloads.config1(nt=2000)
     elif name == "config3":
-        wl = workloads.config3(nt=4000)
+        wl = workloads.config3(nt=4000, **size)
     elif name == "config4":
-        wl = workloads.config4(nt=3000)
+        wl = workloads.config4(nt=3000, **size)
     elif name == "config4_plain":  # the config-4 grid and model with one source
-        wl = workloads.config4(nt=3000, batch=1)
+        wl = workloads.config4(nt=3000, batch=1, **size)
     elif name == "config1_batch64":  # the config-1 grid and model with 64 random sources
         import numpy as _np
         wl = workloads.config1(nt=2000)
@@ -240,7 +245,7 @@ def run_ours(args):
 
     K, W = args.steps, args.warmup
     KP = args.profile_steps
-    wl = make_workload(args.workload, W + K + KP + 1)
+    wl = make_workload(args.workload, W + K + KP + 1, args.grid)
     g = wl.grid
     g.flags |= {"persistent": sesnt.FLAG_PERSISTENT_ELEMENT, "tc_tf32x3": sesnt.FLAG_TC_TF32X3,
                 "tc_bf16x3": sesnt.FLAG_TC_BF16X3, "unstaged": sesnt.FLAG_NO_STAGE}.get(args.element, 0)
@@ -479,7 +484,7 @@ def run_reference(args):
     if RANK != 0:
         return None
     K, W = args.steps, args.warmup
-    wl = make_workload(args.workload, W + K + 1)
+    wl = make_workload(args.workload, W + K + 1, args.grid)
     budget = args.ref_seconds
     rate, n, el, threads = cpu_oracle_rate(wl, budget, max_steps=K, warm=min(W, 2))
     return {"impl": "reference", "metric": METRIC, "value": rate, "unit": METRIC, "n_gpus": WORLD, "steps": K,
@@ -503,6 +508,8 @@ def main():
     ap.add_argument("--workload", default="config2",
                     choices=["config1", "config2", "config3", "config4", "config4_plain", "config1_batch64",
                              "served"])
+    ap.add_argument("--grid", type=int, nargs=3, default=None, metavar=("NX", "NY", "NZ"),
+                    help="elements of a smaller case of configs 2-4 (same generator and kernels), e.g. for ncu")
     ap.add_argument("--requests", type=int, default=40, help="served stream: number of requests")
     ap.add_argument("--rates", type=float, nargs="+", default=[2.0, 8.0], help="served stream: arrivals per second")
     ap.add_argument("--max-active", type=int, default=16, help="served stream: concurrent batches")

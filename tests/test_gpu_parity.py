@@ -198,6 +198,36 @@ def test_visco_elastic_sls(gpu, sesnt_lib, oracle_mod, lpd):
     assert rel_l2(ge[0], gs[0]) > 1e-3
 
 
+@pytest.mark.parametrize("lpd,aniso", [(4, False), (5, True), (6, False), (7, False)])
+def test_visco_elastic_sls_fp64_equals_fp64_oracle(gpu, sesnt_lib, oracle_mod, lpd, aniso):
+    """The default SLS element kernel (staged state, degrees 4-7) in FP64
+    against the FP64 oracle: wavefields and memory variables agree to
+    rounding (1e-10 relative L2), seismograms to float32 output rounding."""
+    wl = with_grid(small_workload(lpd, n_sls=3, aniso=aniso, nt=200), precision=8)
+    with sesnt.Simulation(wl.grid) as sim:
+        workloads.setup(sim, wl)
+        sim.run(1, 200)
+        gs = sim.seismograms()[0].astype(np.float64)
+        gf = {k: sim.field(k, precision=8) for k in FIELDS}
+        gm = [sim.field(sesnt.MEMORY_FIELD0 + c * 3 + q, precision=8) for c in range(6) for q in range(3)]
+    o = oracle_mod.Oracle(wl.grid, 8)
+    oracle_mod.load_workload(o, wl)
+    o.run(200)
+    assert o.visco()
+    os_ = o.seismograms().astype(np.float64)
+    e = rel_l2(gs, os_)
+    print("SLS lpd %d aniso %d FP64: seismograms vs FP64 oracle %.2e" % (lpd, aniso, e))
+    assert np.abs(os_).max() > 0 and e < 1e-7
+    for k, v in FIELDS.items():
+        ef = rel_l2(gf[k], o.field(v).astype(np.float64))
+        assert ef < 1e-10, (k, ef)
+    for x, a in enumerate(gm):
+        b = o.field(13 + x).astype(np.float64)
+        assert np.abs(b).max() > 0
+        assert rel_l2(a, b) < 1e-10, x
+    o.close()
+
+
 def test_anisotropy_and_single_force(gpu, sesnt_lib, oracle_mod):
     for kind in (sesnt.SOURCE_MT, sesnt.SOURCE_SF):
         wl = small_workload(4, aniso=True, kind=kind, nt=300)

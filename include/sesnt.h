@@ -248,8 +248,11 @@ int sesnt_get_seismograms(sesnt_t *h, float *out);
  * [batch][nrec][3] (vx, vy, vz): what receiver_cls%record(it) stores on the
  * host each step in the reference (src/config/receiver.f90:136-142).
  * Synchronous, but it waits only until step `it` is done: later steps
- * already queued keep running while it copies (through the handle's own
- * copy stream). For a Fortran driver that keeps its own traces. */
+ * already queued keep running. The receiver kernel also writes every sample
+ * into a float32 copy in mapped, pinned host memory, so once the step is done
+ * the samples are read from host memory with no device copy. Where mapped
+ * memory is unavailable, they are copied through the handle's own copy
+ * stream. For a Fortran driver that keeps its own traces. */
 int sesnt_get_samples(sesnt_t *h, int it, float *out);
 
 /* Checkpoint and resume (no counterpart in the reference, which keeps no

@@ -780,10 +780,18 @@ __global__ void __launch_bounds__(128) k_receivers(const StepArgs<T> a) {
         acc[c] = x;
     }
     if (lane == 0) {
-        T *out = a.seis + (((size_t)s * a.nrec + r) * 3) * a.nt + (it - 1);
+        const size_t at = (((size_t)s * a.nrec + r) * 3) * a.nt + (it - 1);
+        T *out = a.seis + at;
         out[0] = acc[0];
         out[(size_t)a.nt] = acc[1];
         out[2 * (size_t)a.nt] = acc[2];
+        if (a.seis_host) {
+            // host-mapped copy read by sesnt_get_samples without a device copy
+            float *h = a.seis_host + at;
+            h[0] = (float)acc[0];
+            h[(size_t)a.nt] = (float)acc[1];
+            h[2 * (size_t)a.nt] = (float)acc[2];
+        }
     }
     if (a.rec_xmask) record_extra<N, T>(a, r, s, it, lane, ex, ey, ez, vm);
 }

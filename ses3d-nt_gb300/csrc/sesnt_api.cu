@@ -221,6 +221,11 @@ struct sesnt_handle {
     int *d_rec_elem = nullptr;
     void *d_rec_vm = nullptr, *d_seis = nullptr;
     int nrec_dev = 0;
+    // float32 mirror of d_seis in mapped pinned host memory, written by the
+    // receiver kernel: sesnt_get_samples reads a finished step from it with
+    // no device copy (null if mapped memory could not be had)
+    float *h_seis = nullptr, *h_seis_dev = nullptr;
+    size_t h_seis_n = 0;
     // receiver channels beyond vx, vy, vz: per receiver the device-computed
     // channel bits, first trace slot and rotation-strain slot; per (sim,
     // receiver) the source record of its element
@@ -322,10 +327,16 @@ struct sesnt_handle {
         graph = nullptr;
         graph_steps = 0;
     }
+    void free_seis_mirror() {
+        if (h_seis) cudaFreeHost(h_seis);
+        h_seis = h_seis_dev = nullptr;
+        h_seis_n = 0;
+    }
     ~sesnt_handle() {
         drop_graph();
         if (stream) cudaStreamSynchronize(stream);
         writer.reset();  // writes what is queued, then joins
+        free_seis_mirror();
         for (auto &b : bufs) free_buffer(b.p);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
@@ -359,6 +370,7 @@ struct sesnt_handle {
         a.nsrc = nsrc_rec; a.nt = g.nt; a.n_src_vm = n_src_vm; a.n_src_data = n_src_data; a.src = (const SrcRec *)d_src; a.src_vm = (const T *)d_src_vm;
         a.src_data = (const T *)d_src_data;
         a.nrec = nrec_dev; a.rec_elem = d_rec_elem; a.rec_vm = (const T *)d_rec_vm; a.seis = (T *)d_seis;
+        a.seis_host = h_seis_dev;
         a.d_it = d_it; a.step_off = 0;
         a.persistent = (g.flags & SESNT_FLAG_PERSISTENT_ELEMENT) ? 1 : 0;
         a.pair = (g.flags & SESNT_FLAG_NO_PAIR) ? 0 : 1;
@@ -521,7 +533,8 @@ int zero_state(sesnt_t *h) {
         {h->F, E * 3 * (size_t)h->nuni * h->S},
         {h->d_seis, E * (size_t)h->S * h->rec_elem.size() * 3 * h->g.nt},
         {h->d_xseis, E * (size_t)h->S * h->nxtr * h->g.nt},
-        {h->du, E * 9 * (size_t)h->nloc * h->S}};
+        {h->du, E * 9 * (size_t)h->nloc * h->S},
+        {h->h_seis_dev, h->h_seis_n * sizeof(float)}};
     for (auto &z : zs)
         if (z.p && z.n) {
             cudaError_t e = cudaMemsetAsync(z.p, 0, z.n, h->stream);
@@ -680,6 +693,10 @@ int upload_receivers(sesnt_t *h) {
     // keep already recorded samples of existing receivers
     std::vector<T> old;
     const size_t per = (size_t)3 * h->g.nt;
+    if (h->d_seis) {
+        cudaError_t e = cudaStreamSynchronize(h->stream);  // no step still writes the old buffers
+        if (e != cudaSuccess) return h->cuda_fail(e, "synchronize");
+    }
     if (h->d_seis && h->nrec_dev > 0) {
         old.resize((size_t)h->S * h->nrec_dev * per);
         cudaError_t e = cudaMemcpy(old.data(), h->d_seis, old.size() * sizeof(T), cudaMemcpyDeviceToHost);
@@ -687,6 +704,7 @@ int upload_receivers(sesnt_t *h) {
     }
     h->release(h->d_rec_elem); h->release(h->d_rec_vm); h->release(h->d_seis);
     h->d_rec_elem = nullptr; h->d_rec_vm = h->d_seis = nullptr;
+    h->free_seis_mirror();
     h->nrec_dev = 0;
     if (nrec == 0) return SESNT_OK;
     int rc;
@@ -705,6 +723,17 @@ int upload_receivers(sesnt_t *h) {
     if (e == cudaSuccess) e = cudaMemcpy(h->d_rec_vm, vm.data(), vm.size() * sizeof(T), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(h->d_seis, seis.data(), seis.size() * sizeof(T), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return h->cuda_fail(e, "uploading receivers");
+    void *hm = nullptr, *hd = nullptr;
+    if (cudaHostAlloc(&hm, seis.size() * sizeof(float), cudaHostAllocMapped) == cudaSuccess &&
+        cudaHostGetDevicePointer(&hd, hm, 0) == cudaSuccess) {
+        h->h_seis = (float *)hm;
+        h->h_seis_dev = (float *)hd;
+        h->h_seis_n = seis.size();
+        for (size_t x = 0; x < seis.size(); ++x) h->h_seis[x] = (float)seis[x];
+    } else {
+        if (hm) cudaFreeHost(hm);
+        cudaGetLastError();  // no mirror: sesnt_get_samples copies from the device
+    }
     h->nrec_dev = (int)nrec;
     int rc2 = upload_receiver_channels<T>(h);
     return rc2 ? rc2 : upload_receiver_sources(h);
@@ -1483,12 +1512,24 @@ int sesnt_get_samples(sesnt_t *h, int it, float *out) {
     if (nrec == 0) return SESNT_OK;
     if (h->rec_dirty) return h->fail(SESNT_ESTATE, "receivers added after the last step");
     const size_t E = h->esize, nt = h->g.nt;
-    std::vector<double> tmp(h->S * nrec * 3);
     // wait for step it only (the earliest progress mark at or after it), or
     // for everything queued when no mark covers it
     int best = -1;
     for (int q = 0; q < sesnt_handle::kMarks; ++q)
         if (h->mark_it[q] >= it && (best < 0 || h->mark_it[q] < h->mark_it[best])) best = q;
+    if (best >= 0 && h->h_seis) {
+        // the mark's event follows the receiver kernel of step it: its
+        // mapped-memory writes are visible once the event has completed
+        cudaError_t e = cudaEventSynchronize(h->mark_ev[best]);
+        if (e != cudaSuccess) return h->cuda_fail(e, "reading samples");
+        for (size_t x = 0; x < (size_t)h->S * nrec * 3; ++x) {
+            const size_t r = (x / 3) % nrec;
+            const bool on = (h->rec_mask[r] >> (x % 3)) & 1u;
+            out[x] = on ? h->h_seis[x * nt + (it - 1)] : 0.0f;
+        }
+        return SESNT_OK;
+    }
+    std::vector<double> tmp(h->S * nrec * 3);
     cudaStream_t cs = best >= 0 ? h->copy_stream : h->stream;
     cudaError_t e = best >= 0 ? cudaEventSynchronize(h->mark_ev[best]) : cudaSuccess;
     // one strided 2-D copy: rows [s][r][c] of the seismogram array, column it-1
@@ -1663,6 +1704,16 @@ int sesnt_load_state(sesnt_t *h, const void *buf) {
     for (auto &b : state_buffers(h)) {
         if ((e = cudaMemcpy(b.first, in, b.second, cudaMemcpyHostToDevice)) != cudaSuccess)
             return h->cuda_fail(e, "loading state");
+        if (b.first == h->d_seis && h->h_seis)  // the host mirror of the restored samples
+            for (size_t x = 0; x < h->h_seis_n; ++x) {
+                if (h->esize == 8) {
+                    double v;
+                    std::memcpy(&v, in + x * 8, 8);
+                    h->h_seis[x] = (float)v;
+                } else {
+                    std::memcpy(&h->h_seis[x], in + x * 4, 4);
+                }
+            }
         in += b.second;
     }
     h->last_it = hd.last_it;

@@ -75,6 +75,7 @@ struct StepArgs {
     const int *rec_elem;
     const T *rec_vm;    // [nrec][NP]
     T *seis;            // [S][nrec][3][nt]
+    float *seis_host;   // the same samples in float32, mapped pinned host memory (or null)
     // step counter: it = *d_it + step_off
     const int *d_it;
     int step_off;

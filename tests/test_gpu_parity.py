@@ -346,6 +346,44 @@ def test_samples_read_while_later_steps_run(gpu, sesnt_lib):
             sim.reset()
 
 
+@pytest.mark.parametrize("precision", [4, 8])
+def test_samples_after_checkpoint_load_and_new_receivers(gpu, sesnt_lib, precision):
+    """The per-step samples (read from the host-mapped copy once a step is
+    done) equal the seismograms after a checkpoint is loaded into a fresh
+    handle and stepped on, including the restored steps, and after receivers
+    are added between runs (the earlier samples are kept)."""
+    wl = with_grid(small_workload(4, n_sls=3, nt=90), precision=precision)
+    nrec = len(wl.receivers)
+    with sesnt.Simulation(wl.grid) as sim:
+        workloads.setup(sim, wl)
+        sim.run(1, 40)
+        ck = sim.save_state()
+    with sesnt.Simulation(wl.grid) as sim:
+        workloads.setup(sim, wl)
+        sim.load_state(ck)
+        sim.run(41, 50)
+        got = np.zeros((90, 1, nrec, 3), np.float32)
+        for it in range(1, 91):
+            sim.samples(it, got[it - 1])
+        seis = sim.seismograms()
+    assert np.abs(seis[..., :40]).max() > 0
+    assert np.array_equal(np.moveaxis(got, 0, -1), seis)
+    w2 = copy.copy(wl)
+    w2.receivers = wl.receivers[:2]
+    with sesnt.Simulation(wl.grid) as sim:
+        workloads.setup(sim, w2)
+        sim.run(1, 30)
+        for r in wl.receivers[2:]:
+            sim.add_receiver(*sesnt.locate_point(wl.grid, r.lat, r.lon, r.depth))
+        sim.run(31, 60)
+        got = np.zeros((90, 1, nrec, 3), np.float32)
+        for it in range(1, 91):
+            sim.samples(it, got[it - 1])
+        seis = sim.seismograms()
+    assert np.array_equal(np.moveaxis(got, 0, -1), seis)
+    assert np.abs(seis[0, :2, :, :30]).max() > 0 and not np.any(seis[0, 2:, :, :30])
+
+
 def batched(wl, batch):
     g = copy.copy(wl.grid)
     g.batch = batch

@@ -126,30 +126,75 @@ __global__ void k_tau(const T *q, T *tau, long long n) {
     if (i < n) tau[i] = (T)(6.0814 * pow((double)q[i], -1.015));
 }
 
+// Min, max and a non-finite flag of v (float32 keys), reduced per block
+// (shuffles, then shared memory) so that each block makes one atomic per
+// word; four independent loads per iteration keep memory busy. The last
+// block to finish (counted in mm[3] after a fence) copies the result to
+// `out` (mapped host memory) and resets mm for the next call, so a call is
+// one launch and one synchronisation. No block waits for another.
+// mm: [0] ordered bits of the minimum, [1] of the maximum, [2] non-finite
+// flag, [3] finished blocks; all four start at {~0, 0, 0, 0}. out: the
+// three result words.
 template <typename T>
-__global__ void k_minmax(const T *v, long long n, unsigned long long *mm, int *bad) {
-    // mm[0] = ordered bits of the minimum, mm[1] of the maximum (float32)
+__global__ void __launch_bounds__(256) k_minmax(const T *v, long long n, unsigned long long *mm,
+                                                unsigned long long *out) {
     float lo = INFINITY, hi = -INFINITY;
     int nonfinite = 0;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        float x = (float)v[i];
+    auto take = [&](float x) {
         if (!isfinite(x)) nonfinite = 1;
         lo = fminf(lo, x);
         hi = fmaxf(hi, x);
+    };
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < n; i += 4 * stride) {
+        const float x0 = (float)v[i], x1 = (float)v[i + stride], x2 = (float)v[i + 2 * stride],
+                    x3 = (float)v[i + 3 * stride];
+        take(x0);
+        take(x1);
+        take(x2);
+        take(x3);
     }
+    for (; i < n; i += stride) take((float)v[i]);
     for (int o = 16; o > 0; o >>= 1) {
         lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
         hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
         nonfinite |= __shfl_xor_sync(0xffffffffu, nonfinite, o);
     }
+    __shared__ float slo[8], shi[8];
+    __shared__ int snf[8];
+    const int w = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) {
+        slo[w] = lo;
+        shi[w] = hi;
+        snf[w] = nonfinite;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int q = 1; q < (int)(blockDim.x >> 5); ++q) {
+            lo = fminf(lo, slo[q]);
+            hi = fmaxf(hi, shi[q]);
+            nonfinite |= snf[q];
+        }
         auto key = [](float f) -> unsigned long long {
             unsigned b = __float_as_uint(f);
             return (unsigned long long)((b & 0x80000000u) ? ~b : (b | 0x80000000u));
         };
         atomicMin(&mm[0], key(lo));
         atomicMax(&mm[1], key(hi));
-        if (nonfinite) atomicOr(bad, 1);
+        if (nonfinite) atomicOr(&mm[2], 1ULL);
+        __threadfence();
+        if (atomicAdd(&mm[3], 1ULL) == (unsigned long long)gridDim.x - 1) {
+            // every other block's atomics precede its count: the words are final
+            __threadfence();
+            out[0] = atomicAdd(&mm[0], 0ULL);
+            out[1] = atomicAdd(&mm[1], 0ULL);
+            out[2] = atomicAdd(&mm[2], 0ULL);
+            mm[0] = ~0ULL;
+            mm[1] = 0ULL;
+            mm[2] = 0ULL;
+            mm[3] = 0ULL;
+        }
     }
 }
 
@@ -253,6 +298,10 @@ struct sesnt_handle {
     // graph
     cudaGraphExec_t graph = nullptr;
     int graph_steps = 0;
+    cudaGraphExec_t graph1 = nullptr;  // one step, for sesnt_step
+    // v_ptp: device reduction words and the mapped host words of the result
+    unsigned long long *d_ptp = nullptr, *h_ptp = nullptr, *h_ptp_dev = nullptr;
+
     // events for timing
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int launches_per_step = 0;
@@ -326,6 +375,8 @@ struct sesnt_handle {
         if (graph) cudaGraphExecDestroy(graph);
         graph = nullptr;
         graph_steps = 0;
+        if (graph1) cudaGraphExecDestroy(graph1);
+        graph1 = nullptr;
     }
     void free_seis_mirror() {
         if (h_seis) cudaFreeHost(h_seis);
@@ -337,6 +388,7 @@ struct sesnt_handle {
         if (stream) cudaStreamSynchronize(stream);
         writer.reset();  // writes what is queued, then joins
         free_seis_mirror();
+        if (h_ptp) cudaFreeHost(h_ptp);
         for (auto &b : bufs) free_buffer(b.p);
         if (ev0) cudaEventDestroy(ev0);
         if (ev1) cudaEventDestroy(ev1);
@@ -803,26 +855,35 @@ int enqueue_steps(sesnt_t *h, int n, bool rot_full = false) {
 
 constexpr int kGraphSteps = 32;
 
+// Captures n steps (n = kGraphSteps: advancing the step counter by n at the
+// end; n = 1: the step at the counter, for sesnt_step) into *exec.
 template <typename T>
-int build_graph(sesnt_t *h) {
-    h->drop_graph();
+int capture_steps(sesnt_t *h, int n, cudaGraphExec_t *exec) {
     cudaGraph_t gr = nullptr;
     cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return h->cuda_fail(e, "cudaStreamBeginCapture");
-    int rc = enqueue_steps<T>(h, kGraphSteps);
-    if (!rc) k_advance_it<<<1, 1, 0, h->stream>>>(h->d_it, kGraphSteps);
+    int rc = enqueue_steps<T>(h, n);
+    if (!rc && n > 1) k_advance_it<<<1, 1, 0, h->stream>>>(h->d_it, n);
     e = cudaStreamEndCapture(h->stream, &gr);
     if (rc) {
         if (gr) cudaGraphDestroy(gr);
         return rc;
     }
     if (e != cudaSuccess) return h->cuda_fail(e, "cudaStreamEndCapture");
-    e = cudaGraphInstantiate(&h->graph, gr, 0);
+    e = cudaGraphInstantiate(exec, gr, 0);
     cudaGraphDestroy(gr);
     if (e != cudaSuccess) {
-        h->graph = nullptr;
+        *exec = nullptr;
         return h->cuda_fail(e, "cudaGraphInstantiate");
     }
+    return SESNT_OK;
+}
+
+template <typename T>
+int build_graph(sesnt_t *h) {
+    h->drop_graph();
+    int rc = capture_steps<T>(h, kGraphSteps, &h->graph);
+    if (rc) return rc;
     h->graph_steps = kGraphSteps;
     return SESNT_OK;
 }
@@ -841,6 +902,14 @@ int run_steps(sesnt_t *h, int it0, int nsteps) {
             left -= kGraphSteps;
             h->mark(it0 + nsteps - left - 1);
         }
+    }
+    if (left == 1 && h->use_graph) {
+        // a single step (the sesnt_step loop of a driver): one graph launch
+        if (!h->graph1 && (rc = capture_steps<T>(h, 1, &h->graph1))) return rc;
+        cudaError_t e = cudaGraphLaunch(h->graph1, h->stream);
+        if (e != cudaSuccess) return h->cuda_fail(e, "cudaGraphLaunch");
+        h->mark(it0 + nsteps - 1);
+        left = 0;
     }
     if (left > 0) {
         if ((rc = enqueue_steps<T>(h, left))) return rc;
@@ -1150,27 +1219,40 @@ int get_seis_impl(sesnt_t *h, float *out) {
 
 template <typename T>
 int v_ptp_impl(sesnt_t *h, int sim, float out[2]) {
-    unsigned long long *mm = nullptr;
     int rc;
-    if ((rc = h->alloc((void **)&mm, 2 * sizeof(unsigned long long) + sizeof(int), "ptp"))) return rc;
-    unsigned long long init[2] = {~0ULL, 0ULL};
-    int zero = 0;
-    cudaError_t e = cudaMemcpy(mm, init, sizeof init, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(mm + 2, &zero, sizeof zero, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) {
-        k_minmax<T><<<4 * 152, 256, 0, h->stream>>>((const T *)h->v + (size_t)sim * 3 * h->nuni,
-                                                    3 * h->nuni, mm, (int *)(mm + 2));
-        e = cudaStreamSynchronize(h->stream);
+    // per call: reduce and copy back on the handle's stream, one
+    // synchronisation; the words live in the handle
+    if (!h->h_ptp) {
+        void *hm = nullptr, *hd = nullptr;
+        if (cudaHostAlloc(&hm, 3 * sizeof(unsigned long long), cudaHostAllocMapped) != cudaSuccess ||
+            cudaHostGetDevicePointer(&hd, hm, 0) != cudaSuccess) {
+            if (hm) cudaFreeHost(hm);
+            cudaGetLastError();
+            return h->fail(SESNT_ENOMEM, "mapped host words for v_ptp");
+        }
+        h->h_ptp = (unsigned long long *)hm;
+        h->h_ptp_dev = (unsigned long long *)hd;
     }
-    unsigned long long res[2];
-    int bad = 0;
-    if (e == cudaSuccess) e = cudaMemcpy(res, mm, sizeof res, cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess) e = cudaMemcpy(&bad, mm + 2, sizeof bad, cudaMemcpyDeviceToHost);
-    h->release(mm);
-    if (e != cudaSuccess) return h->cuda_fail(e, "v_ptp");
-    out[0] = unkey(res[0]);
-    out[1] = unkey(res[1]);
-    if (bad) return h->fail(SESNT_ENONFINITE, "wavefield of simulation %d contains NaN or Inf", sim);
+    if (!h->d_ptp) {
+        if ((rc = h->alloc((void **)&h->d_ptp, 4 * sizeof(unsigned long long), "ptp"))) return rc;
+        const unsigned long long init[4] = {~0ULL, 0ULL, 0ULL, 0ULL};
+        cudaError_t e = cudaMemcpy(h->d_ptp, init, sizeof init, cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) return h->cuda_fail(e, "v_ptp");
+    }
+    // 8 blocks of 256 threads per SM, each thread 4 loads in flight
+    k_minmax<T><<<8 * 152, 256, 0, h->stream>>>((const T *)h->v + (size_t)sim * 3 * h->nuni, 3 * h->nuni, h->d_ptp,
+                                                h->h_ptp_dev);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) {
+        // the words may be left mid-reduction: set them up again next call
+        h->release(h->d_ptp);
+        h->d_ptp = nullptr;
+        return h->cuda_fail(e, "v_ptp");
+    }
+    out[0] = unkey(h->h_ptp[0]);
+    out[1] = unkey(h->h_ptp[1]);
+    if (h->h_ptp[2]) return h->fail(SESNT_ENONFINITE, "wavefield of simulation %d contains NaN or Inf", sim);
     return SESNT_OK;
 }
 

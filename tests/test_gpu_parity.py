@@ -384,6 +384,39 @@ def test_samples_after_checkpoint_load_and_new_receivers(gpu, sesnt_lib, precisi
     assert np.abs(seis[0, :2, :, :30]).max() > 0 and not np.any(seis[0, 2:, :, :30])
 
 
+@pytest.mark.parametrize("precision", [4, 8])
+def test_v_ptp_every_step(gpu, sesnt_lib, precision):
+    """v_ptp asked every step, as the reference driver's loop does
+    (src/ses3d-nt.F90:240-270; one reduction launch per call, its words
+    reset by the kernel itself): it equals min/max of the velocity fields read
+    back, per simulation of a batch, also after a reset and after a
+    checkpoint load."""
+    wl = batched(with_grid(small_workload(4, n_sls=3, nt=60), precision=precision), 2)
+
+    def direct(sim, s):
+        f = [sim.field(k, sim=s) for k in ("vx", "vy", "vz")]
+        return min(x.min() for x in f), max(x.max() for x in f)
+
+    with sesnt.Simulation(wl.grid) as sim:
+        workloads.setup(sim, wl)
+        ck = None
+        for it in range(1, 61):
+            sim.step(it)
+            for s in range(2):
+                lo, hi = sim.v_ptp(s)
+                if it in (1, 2, 17, 40, 60):
+                    assert (lo, hi) == direct(sim, s), (it, s)
+            if it == 30:
+                ck = sim.save_state()
+        assert direct(sim, 1)[1] > 0
+        sim.reset()
+        assert sim.v_ptp(0) == (0.0, 0.0)
+        sim.load_state(ck)
+        assert sim.v_ptp(1) == direct(sim, 1)
+        sim.run(31, 10)
+        assert sim.v_ptp(1) == direct(sim, 1)
+
+
 def batched(wl, batch):
     g = copy.copy(wl.grid)
     g.batch = batch

@@ -268,9 +268,12 @@ struct sesnt_handle {
     int nrec_dev = 0;
     // float32 mirror of d_seis in mapped pinned host memory, written by the
     // receiver kernel: sesnt_get_samples reads a finished step from it with
-    // no device copy (null if mapped memory could not be had)
+    // no device copy. Made with the receiver upload when it takes at most
+    // kEagerMirrorBytes, else by the first sesnt_get_samples call (null
+    // until then, or if mapped memory could not be had: seis_mirror_failed).
     float *h_seis = nullptr, *h_seis_dev = nullptr;
     size_t h_seis_n = 0;
+    bool seis_mirror_failed = false;
     // receiver channels beyond vx, vy, vz: per receiver the device-computed
     // channel bits, first trace slot and rotation-strain slot; per (sim,
     // receiver) the source record of its element
@@ -737,6 +740,11 @@ int upload_receiver_sources(sesnt_t *h) {
     return e == cudaSuccess ? SESNT_OK : h->cuda_fail(e, "uploading receiver sources");
 }
 
+// Host mirrors of the seismograms up to this size are made with the
+// receiver upload; larger ones (batched runs with many receivers and steps)
+// only when per-step samples are first read.
+constexpr size_t kEagerMirrorBytes = 16u << 20;
+
 template <typename T>
 int upload_receivers(sesnt_t *h) {
     h->rec_dirty = false;
@@ -775,16 +783,19 @@ int upload_receivers(sesnt_t *h) {
     if (e == cudaSuccess) e = cudaMemcpy(h->d_rec_vm, vm.data(), vm.size() * sizeof(T), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(h->d_seis, seis.data(), seis.size() * sizeof(T), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return h->cuda_fail(e, "uploading receivers");
-    void *hm = nullptr, *hd = nullptr;
-    if (cudaHostAlloc(&hm, seis.size() * sizeof(float), cudaHostAllocMapped) == cudaSuccess &&
-        cudaHostGetDevicePointer(&hd, hm, 0) == cudaSuccess) {
-        h->h_seis = (float *)hm;
-        h->h_seis_dev = (float *)hd;
-        h->h_seis_n = seis.size();
-        for (size_t x = 0; x < seis.size(); ++x) h->h_seis[x] = (float)seis[x];
-    } else {
-        if (hm) cudaFreeHost(hm);
-        cudaGetLastError();  // no mirror: sesnt_get_samples copies from the device
+    h->seis_mirror_failed = false;
+    if (seis.size() * sizeof(float) <= kEagerMirrorBytes) {
+        void *hm = nullptr, *hd = nullptr;
+        if (cudaHostAlloc(&hm, seis.size() * sizeof(float), cudaHostAllocMapped) == cudaSuccess &&
+            cudaHostGetDevicePointer(&hd, hm, 0) == cudaSuccess) {
+            h->h_seis = (float *)hm;
+            h->h_seis_dev = (float *)hd;
+            h->h_seis_n = seis.size();
+            for (size_t x = 0; x < seis.size(); ++x) h->h_seis[x] = (float)seis[x];
+        } else {
+            if (hm) cudaFreeHost(hm);
+            cudaGetLastError();  // made (or given up) at the first sesnt_get_samples
+        }
     }
     h->nrec_dev = (int)nrec;
     int rc2 = upload_receiver_channels<T>(h);
@@ -1586,6 +1597,40 @@ int sesnt_run_profiled(sesnt_t *h, int it0, int nsteps, float ms[4]) {
     return err == cudaSuccess ? h->wait_status() : h->cuda_fail(err, "profiled run");
 }
 
+// The host mirror of the seismograms (see sesnt_handle::h_seis): made from
+// the device array once all queued steps are done; the captured steps are
+// dropped so that the next ones write to it too.
+int make_seis_mirror(sesnt_t *h) {
+    const size_t n = (size_t)h->S * h->rec_elem.size() * 3 * h->g.nt, E = h->esize;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "synchronize");
+    void *hm = nullptr, *hd = nullptr;
+    std::vector<char> dev(n * E);
+    if (cudaHostAlloc(&hm, n * sizeof(float), cudaHostAllocMapped) != cudaSuccess ||
+        cudaHostGetDevicePointer(&hd, hm, 0) != cudaSuccess ||
+        cudaMemcpy(dev.data(), h->d_seis, n * E, cudaMemcpyDeviceToHost) != cudaSuccess) {
+        if (hm) cudaFreeHost(hm);
+        cudaGetLastError();
+        h->seis_mirror_failed = true;  // sesnt_get_samples copies from the device
+        return SESNT_OK;
+    }
+    float *f = (float *)hm;
+    for (size_t x = 0; x < n; ++x) {
+        if (E == 8) {
+            double v;
+            std::memcpy(&v, dev.data() + x * 8, 8);
+            f[x] = (float)v;
+        } else {
+            std::memcpy(&f[x], dev.data() + x * 4, 4);
+        }
+    }
+    h->h_seis = f;
+    h->h_seis_dev = (float *)hd;
+    h->h_seis_n = n;
+    h->drop_graph();
+    return SESNT_OK;
+}
+
 int sesnt_get_samples(sesnt_t *h, int it, float *out) {
     if (!h || !out) return SESNT_EINVAL;
     Range r("sesnt_get_samples");
@@ -1594,6 +1639,8 @@ int sesnt_get_samples(sesnt_t *h, int it, float *out) {
     if (nrec == 0) return SESNT_OK;
     if (h->rec_dirty) return h->fail(SESNT_ESTATE, "receivers added after the last step");
     const size_t E = h->esize, nt = h->g.nt;
+    int rc;
+    if (!h->h_seis && !h->seis_mirror_failed && h->d_seis && (rc = make_seis_mirror(h))) return rc;
     // wait for step it only (the earliest progress mark at or after it), or
     // for everything queued when no mark covers it
     int best = -1;

@@ -384,6 +384,27 @@ def test_samples_after_checkpoint_load_and_new_receivers(gpu, sesnt_lib, precisi
     assert np.abs(seis[0, :2, :, :30]).max() > 0 and not np.any(seis[0, 2:, :, :30])
 
 
+def test_samples_of_a_large_receiver_set(gpu, sesnt_lib):
+    """Seismogram arrays above the eager size of the host copy (here 2 x 60
+    receivers x 12000 steps, 17 MB) get it at the first per-step read: the
+    samples equal the seismograms before and after it exists."""
+    wl = batched(small_workload(4, nt=12000), 2)
+    wl.receivers = [workloads.Receiver(lat=31.0 + 0.13 * q, lon=1.0 + 0.13 * q, depth=1000.0 * (q % 7))
+                    for q in range(60)]
+    with sesnt.Simulation(wl.grid) as sim:
+        workloads.setup(sim, wl)
+        got = np.zeros((80, 2, 60, 3), np.float32)
+        sim.run(1, 40)
+        for it in range(1, 41):
+            sim.samples(it, got[it - 1])
+        sim.run(41, 40)
+        for it in range(41, 81):
+            sim.samples(it, got[it - 1])
+        seis = sim.seismograms()[..., :80]
+    assert np.abs(seis).max() > 0
+    assert np.array_equal(np.moveaxis(got, 0, -1), seis)
+
+
 @pytest.mark.parametrize("precision", [4, 8])
 def test_v_ptp_every_step(gpu, sesnt_lib, precision):
     """v_ptp asked every step, as the reference driver's loop does

@@ -206,7 +206,8 @@ int sesnt_add_receiver(sesnt_t *h, int ex, int ey, int ez, const float *vanderm,
 
 /* One pass of the reference forward loop body for step `it` (1..nt):
  * ses3d_evolution, then source add(it), then receiver record(it)
- * (src/ses3d-nt.F90:240-250). Asynchronous on the handle's stream. */
+ * (src/ses3d-nt.F90:240-250). Asynchronous on the handle's stream; replayed
+ * from a captured one-step CUDA graph unless SESNT_FLAG_NO_GRAPH is set. */
 int sesnt_step(sesnt_t *h, int it);
 
 /* Steps it0 .. it0+nsteps-1. Long runs are replayed from a captured CUDA
@@ -304,7 +305,8 @@ int sesnt_get_field(sesnt_t *h, int sim, int which, void *out, int out_precision
 /* Global minimum and maximum of the velocity components of simulation `sim`,
  * the quantity the reference prints every step (v_ptp_glb,
  * src/elastic_vars.F90:179-213). Returns SESNT_ENONFINITE if any value is
- * NaN or Inf. Synchronous. */
+ * NaN or Inf. Synchronous: one reduction launch on the handle's stream,
+ * whose result arrives in mapped host memory. */
 int sesnt_v_ptp(sesnt_t *h, int sim, float out[2]);
 
 /* Sums an element-local field over every copy of each shared GLL point and

@@ -82,9 +82,8 @@ __global__ void __launch_bounds__(256) k_derived(const StepArgs<T> a, int which,
     if (which == SESNT_FIELD_PRESSURE) {
         // -1.0*(sxx + syy + szz)/3.0 on the stored stresses (xx xy xz yy yz zz)
         const size_t e = li / NP, p = li % NP;
-        constexpr int NPS = state_stride(NP);
-        const T *sg = a.sig + (e * a.S + sim) * 6 * NPS + p;
-        out = (T(-1) * (sg[0] + sg[3 * NPS] + sg[5 * NPS])) / T(3);
+        const T *sg = a.sig + (e * a.S + sim) * (size_t)a.st_unit + p;
+        out = (T(-1) * (sg[0] + sg[3 * a.st_cs] + sg[5 * a.st_cs])) / T(3);
     } else if (which >= SESNT_FIELD_EXX && which <= SESNT_FIELD_EZZ) {
         const T *du = a.du + (size_t)sim * 9 * nloc + li;
         switch (which) {

@@ -209,9 +209,9 @@ __global__ void __launch_bounds__(TcCfg<N, PREC>::NT) k_element_tc(const StepArg
     size_t u = 0;
     T vx = 0, vy = 0, vz = 0, lam = 0, mu = 0, tau = 0, cA = 0, cB = 0, cC = 0;
     T sg[6] = {0, 0, 0, 0, 0, 0}, m[6][MS];
-    constexpr int NPS = state_stride(NP);  // element-blocked [e][s][comp][NPS]
-    T *sig = a.sig + ((size_t)e * S + s) * 6 * NPS + p;
-    T *mem = a.mem + ((size_t)e * S + s) * 6 * MS * NPS + p;
+    constexpr int NPS = StateLayout<NP, NSLS>::CS;  // element-blocked units (StateLayout)
+    T *sig = a.sig + ((size_t)e * S + s) * StateLayout<NP, NSLS>::UNIT + p;
+    T *mem = a.mem + ((size_t)e * S + s) * StateLayout<NP, NSLS>::UNIT + p;
     if (act && in_range(unique_index<N>(a.NXU, a.NYU, ex, ey, ez, i, j, k), nuni, a.err) &&
         in_range(li, nloc, a.err)) {
         u = unique_index<N>(a.NXU, a.NYU, ex, ey, ez, i, j, k);

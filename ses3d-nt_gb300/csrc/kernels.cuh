@@ -387,15 +387,16 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::M
     T lam = 0, mu = 0, tau = 0, cA = 0, cB = 0, cC = 0;
     T sg[6] = {0, 0, 0, 0, 0, 0};
     T m[6][MS];
-    // stress and memory variables: element-blocked [e][s][comp][NPS]
-    constexpr int NPS = state_stride(NP);
+    // stress and memory variables: element-blocked units (StateLayout)
+    constexpr int NPS = StateLayout<NP, NSLS>::CS;
+    constexpr size_t UNIT = StateLayout<NP, NSLS>::UNIT;
     const size_t sb = (size_t)e * S + s;
-    T *sig = a.sig + sb * 6 * NPS + p;
-    T *mem = a.mem + sb * 6 * MS * NPS + p;
+    T *sig = a.sig + sb * UNIT + p;
+    T *mem = a.mem + sb * UNIT + p;
     act = act && in_range(unique_index<N>(a.NXU, a.NYU, e % a.nx, (e / a.nx) % a.ny, e / (a.nx * a.ny), i, j, k),
                           nuni, a.err) &&
-          in_range(li, nloc, a.err) && in_range(sb * 6 * NPS + 5 * NPS + p, (size_t)a.nel * S * 6 * NPS, a.err) &&
-          (NSLS == 0 || in_range(sb * 6 * MS * NPS + (6 * MS - 1) * NPS + p, (size_t)a.nel * S * 6 * MS * NPS, a.err));
+          in_range(li, nloc, a.err) && in_range(sb * UNIT + 5 * NPS + p, (size_t)a.nel * S * UNIT, a.err) &&
+          (NSLS == 0 || in_range(sb * UNIT + 6 * NPS + (6 * MS - 1) * NPS + p, (size_t)a.nel * S * UNIT, a.err));
     if (act) {
         ex = e % a.nx;
         ey = (e / a.nx) % a.ny;

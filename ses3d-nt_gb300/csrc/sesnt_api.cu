@@ -65,14 +65,15 @@ struct Range {
 __global__ void k_set_it(int *d_it, int v) { *d_it = v; }
 
 // One component of the element-blocked stress / memory-variable state
-// [e][s][ncomp][NP] as an element-local field [e][NP] of simulation `sim`.
+// (StateLayout: `unit` values per (element, simulation), components `cs`
+// apart from `src`) as an element-local field [e][NP] of simulation `sim`.
 template <typename T>
-__global__ void k_extract(const T *__restrict__ src, int S, int ncomp, int sim, int c, int NP, long long nel,
-                          T *__restrict__ out) {
+__global__ void k_extract(const T *__restrict__ src, int S, long long unit, int cs, int sim, int c, int NP,
+                          long long nel, T *__restrict__ out) {
     const size_t li = (size_t)blockIdx.x * 256 + threadIdx.x;
     if (li >= (size_t)nel * NP) return;
     const size_t e = li / NP, p = li % NP;
-    out[li] = src[((e * S + sim) * ncomp + c) * (size_t)state_stride(NP) + p];
+    out[li] = src[(e * S + sim) * (size_t)unit + (size_t)c * cs + p];
 }
 __global__ void k_advance_it(int *d_it, int by) { *d_it += by; }
 
@@ -374,6 +375,9 @@ struct sesnt_handle {
         mark_it[mark_next] = it;
         mark_next = (mark_next + 1) % kMarks;
     }
+    // layout of the stress and memory-variable units (StateLayout)
+    size_t state_unit() const { return sesnt::state_unit(NP, sls ? kNsls : 0); }
+    int state_cs() const { return sesnt::state_cs(NP, sls); }
     void drop_graph() {
         if (graph) cudaGraphExecDestroy(graph);
         graph = nullptr;
@@ -422,6 +426,7 @@ struct sesnt_handle {
         a.lam = (const T *)lam; a.mu = (const T *)mu; a.A = (const T *)A; a.B = (const T *)B; a.C = (const T *)C;
         a.tau = (const T *)tau;
         a.sig = (T *)sig; a.mem = (T *)mem; a.v = (T *)v; a.vc = (T *)vc; a.F = (T *)F; a.invM = (const T *)invM;
+        a.st_cs = state_cs(); a.st_unit = (long long)state_unit();
         a.nsrc = nsrc_rec; a.nt = g.nt; a.n_src_vm = n_src_vm; a.n_src_data = n_src_data; a.src = (const SrcRec *)d_src; a.src_vm = (const T *)d_src_vm;
         a.src_data = (const T *)d_src_data;
         a.nrec = nrec_dev; a.rec_elem = d_rec_elem; a.rec_vm = (const T *)d_rec_vm; a.seis = (T *)d_seis;
@@ -581,8 +586,7 @@ const LpdOps<T> *ops(const sesnt_t *h) {
 int zero_state(sesnt_t *h) {
     const size_t E = h->esize;
     struct Z { void *p; size_t n; } zs[] = {
-        {h->sig, E * 6 * (size_t)h->nel * state_stride(h->NP) * h->S},
-        {h->mem, h->sls ? E * 6 * kNsls * (size_t)h->nel * state_stride(h->NP) * h->S : 0},
+        {h->sig, E * h->state_unit() * (size_t)h->nel * h->S},  // with the memory variables (StateLayout)
         {h->v, E * 3 * (size_t)h->nuni * h->S},
         {h->vc, h->kahan ? E * 3 * (size_t)h->nuni * h->S : 0},
         {h->F, E * 3 * (size_t)h->nuni * h->S},
@@ -962,8 +966,8 @@ int field_source(sesnt_t *h, int sim, int which, T *scratch, const T **out, bool
     if (which >= 0 && which <= 2) {
         rc = o->gather_local(a, (const T *)h->v + ((size_t)sim * 3 + which) * nuni, scratch, h->stream);
     } else if (which >= 3 && which <= 8) {
-        k_extract<T><<<(unsigned)((nloc + 255) / 256), 256, 0, h->stream>>>((const T *)h->sig, h->S, 6, sim,
-                                                                             which - 3, h->NP, h->nel, scratch);
+        k_extract<T><<<(unsigned)((nloc + 255) / 256), 256, 0, h->stream>>>(
+            (const T *)h->sig, h->S, (long long)h->state_unit(), h->state_cs(), sim, which - 3, h->NP, h->nel, scratch);
         rc = cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
     } else if (which == SESNT_FIELD_TAPER) {
         rc = o->taper_local(a, scratch, h->stream);
@@ -973,7 +977,8 @@ int field_source(sesnt_t *h, int sim, int which, T *scratch, const T **out, bool
     } else if (which >= SESNT_FIELD_MEMORY && which < SESNT_FIELD_MEMORY + 6 * kNsls && h->sls) {
         // memory variable (component c, mechanism q) at slot c*kNsls + q
         k_extract<T><<<(unsigned)((nloc + 255) / 256), 256, 0, h->stream>>>(
-            (const T *)h->mem, h->S, 6 * kNsls, sim, which - SESNT_FIELD_MEMORY, h->NP, h->nel, scratch);
+            (const T *)h->mem, h->S, (long long)h->state_unit(), h->state_cs(), sim, which - SESNT_FIELD_MEMORY, h->NP,
+            h->nel, scratch);
         rc = cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
     } else if (which == SESNT_FIELD_PRESSURE) {
         rc = o->derived(a, which, sim, nullptr, scratch, h->stream);
@@ -1301,7 +1306,7 @@ size_t footprint(const sesnt_grid_t *g, bool aniso) {
     const size_t E = g->precision == 8 ? 8 : 4, S = g->batch;
     size_t b = 0;
     b += nloc * E * (2 + (aniso ? 3 : 0) + (g->n_sls ? 1 : 0));    // lambda, mu, A,B,C, tau
-    b += nel * state_stride((int)NP) * E * S * (6 + (g->n_sls ? 6 * kNsls : 0));  // sigma, memory
+    b += nel * state_unit((int)NP, g->n_sls ? kNsls : 0) * E * S;  // sigma and memory variables (StateLayout)
     b += nuni * E * (1 + S * (6 + ((g->flags & SESNT_FLAG_KAHAN) ? 3 : 0)));  // invM, v, F, comp
     b += nloc * E * S * (((g->flags & SESNT_FLAG_STRAIN) ? 9 : 0) + ((g->flags & SESNT_FLAG_ROTATION) ? 6 : 0));
     b += nloc * (sizeof(float) + E);                                // set_model staging + rhoinv (transient)
@@ -1375,7 +1380,7 @@ int sesnt_create(const sesnt_grid_t *grid, sesnt_t **out) {
         {(void **)&h->dsin, grid->nx * P * 8, "dsin"}, {(void **)&h->dr, grid->nz * P * 8, "dr"},
         {(void **)&h->dw, P * 8, "dw"},
         {&h->lam, nloc * E, "lambda"}, {&h->mu, nloc * E, "mu"},
-        {&h->sig, 6 * (size_t)h->nel * state_stride(h->NP) * E * S, "stress"},
+        {&h->sig, h->state_unit() * (size_t)h->nel * E * S, "stress and memory variables"},
         {&h->v, 3 * nuni * E * S, "velocity"}, {&h->F, 3 * nuni * E * S, "force"},
         {&h->invM, nuni * E, "inverse mass"}, {(void **)&h->d_it, sizeof(int), "step counter"},
         {(void **)&h->d_err, sizeof(int), "error word"}};
@@ -1385,7 +1390,9 @@ int sesnt_create(const sesnt_grid_t *grid, sesnt_t **out) {
             return rc;
         }
     if (h->sls) {
-        if ((rc = h->alloc(&h->tau, nloc * E, "tau")) || (rc = h->alloc(&h->mem, 6 * kNsls * (size_t)h->nel * state_stride(h->NP) * E * S, "memory"))) {
+        // the memory variables follow the stress inside each unit (StateLayout)
+        h->mem = (char *)h->sig + (size_t)6 * h->state_cs() * E;
+        if ((rc = h->alloc(&h->tau, nloc * E, "tau"))) {
             g_create_error = h->err;
             return rc;
         }
@@ -1763,9 +1770,9 @@ struct StateHeader {
 };
 
 std::vector<std::pair<void *, size_t>> state_buffers(sesnt_t *h) {
-    const size_t E = h->esize, S = h->S, NPS = state_stride(h->NP), nel = h->nel, nuni = h->nuni;
-    std::vector<std::pair<void *, size_t>> b = {{h->v, 3 * nuni * E * S}, {h->sig, 6 * nel * NPS * E * S}};
-    if (h->mem) b.push_back({h->mem, 6 * kNsls * nel * NPS * E * S});
+    const size_t E = h->esize, S = h->S, nel = h->nel, nuni = h->nuni;
+    // stress with the memory variables (StateLayout)
+    std::vector<std::pair<void *, size_t>> b = {{h->v, 3 * nuni * E * S}, {h->sig, h->state_unit() * nel * E * S}};
     if (h->vc) b.push_back({h->vc, 3 * nuni * E * S});
     if (h->du) b.push_back({h->du, 9 * (size_t)h->nloc * E * S});
     if (h->d_seis) b.push_back({h->d_seis, S * h->rec_elem.size() * 3 * (size_t)h->g.nt * E});

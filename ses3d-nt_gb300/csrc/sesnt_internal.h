@@ -75,6 +75,8 @@ struct StepArgs {
     const int *rec_elem;
     const T *rec_vm;    // [nrec][NP]
     T *seis;            // [S][nrec][3][nt]
+    int st_cs;          // state layout (StateLayout): component stride
+    long long st_unit;  // and values per (element, simulation) unit
     float *seis_host;   // the same samples in float32, mapped pinned host memory (or null)
     // step counter: it = *d_it + step_off
     const int *d_it;
@@ -100,7 +102,7 @@ struct StepArgs {
     int nxtr, nrot;
 };
 
-// Points per element in the element-blocked stress / memory-variable state
+// Points per element in the element-blocked stress of elastic handles
 // [e][s][comp][NPS]: NP padded to a multiple of 4 so that every chunk starts
 // on a 16-byte boundary (coalesced warps, bulk-copy alignment).
 #ifdef __CUDACC__
@@ -109,6 +111,25 @@ struct StepArgs {
 #define SESNT_HD
 #endif
 SESNT_HD constexpr int state_stride(int np) { return (np + 3) & ~3; }
+
+// The state of one (element, simulation) unit, element-blocked: the stress
+// [6][CS], then for visco-elastic handles the memory variables [6*NSLS][CS]
+// (the handle's mem pointer is sig + 6*CS), one contiguous unit that one
+// bulk copy moves. CS is NP padded to a multiple of 4, so that every
+// component chunk starts on a 16-byte boundary for per-thread access, except
+// for visco-elastic degree 4 (NP = 125). There the default kernel moves the
+// state only as whole units by bulk copy, 24*125*4 bytes is a multiple of 16,
+// and padding would cost 2.4% of the state bytes (measured 1.1% of the step).
+// Degree 6, whose kernel stores per thread, measured 4.7% slower unpadded.
+SESNT_HD constexpr int state_cs(int np, bool sls) { return sls && np == 125 ? np : state_stride(np); }
+SESNT_HD constexpr size_t state_unit(int np, int nsls) {
+    return (size_t)(6 + 6 * nsls) * state_cs(np, nsls > 0);
+}
+template <int NP, int NSLS>
+struct StateLayout {
+    static constexpr int CS = state_cs(NP, NSLS > 0);  // component stride
+    static constexpr size_t UNIT = state_unit(NP, NSLS);  // values per unit
+};
 
 // Displacement-gradient components (src/evolution.f90:179-187).
 enum { kDuXX = 0, kDuYY, kDuZZ, kDuXY, kDuYX, kDuXZ, kDuZX, kDuYZ, kDuZY };

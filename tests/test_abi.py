@@ -87,3 +87,32 @@ def test_footprint_and_algorithmic_bytes(sesnt_lib):
     # sigma + 18 memory variables + lambda, mu, tau per local point, 7 per unique point
     assert fp > g.n_loc * 4 * 27
     assert fp < g.n_loc * 4 * 40 + g.n_uni * 4 * 10 + (2 << 20)
+
+
+def test_binding_constants_match_the_header():
+    """Every value #defined in include/sesnt.h (error codes, flags, source
+    kinds, wavelets, receiver channel bits, field ids) equals the Python
+    binding's constant of the same name; every flag and channel bit has one."""
+    import re
+
+    import sesnt
+    defines = {}
+    for line in open(sesnt.HEADER):
+        m = re.match(r"#define\s+SESNT_([A-Z0-9_]+)\s+\(?(-?\d+)u?\)?", line)
+        if m:
+            defines[m.group(1)] = int(m.group(2))
+    assert defines["FLAG_NO_STAGE"] == 256 and defines["ENONFINITE"] == -9
+    for name, value in defines.items():
+        if name.startswith("FIELD_"):
+            key = name[len("FIELD_"):].lower()
+            if key == "memory":
+                assert sesnt.MEMORY_FIELD0 == value
+            else:
+                assert sesnt.FIELDS[key] == value, name
+        elif name.startswith("WAVELET_"):
+            key = name[len("WAVELET_"):]
+            assert sesnt.WAVELETS["SIN**3" if key == "SIN3" else key] == value, name
+        else:
+            assert getattr(sesnt, name) == value, name
+    for prefix in ("FLAG_", "CH_"):
+        assert {n for n in dir(sesnt) if n.startswith(prefix)} == {n for n in defines if n.startswith(prefix)}

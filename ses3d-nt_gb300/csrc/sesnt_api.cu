@@ -120,11 +120,26 @@ __global__ void k_check_model(const float *__restrict__ x, long long n, int mode
     }
 }
 
-// tau = 6.0814 * q^-1.015 (src/model_paras.F90:407), evaluated in FP64.
+// tau = 6.0814 * q^-1.015 (src/model_paras.F90:407), evaluated in FP64, in
+// place over the element-major q. One thread per element walks its NP
+// points and evaluates the power only where q differs from the previous
+// point's, so a per-element Q costs one FP64 pow per element; equal inputs
+// reuse the identical result.
 template <typename T>
-__global__ void k_tau(const T *q, T *tau, long long n) {
-    long long i = (long long)blockIdx.x * 256 + threadIdx.x;
-    if (i < n) tau[i] = (T)(6.0814 * pow((double)q[i], -1.015));
+__global__ void k_tau(const T *q, T *tau, long long nel, int NP) {
+    const long long e = (long long)blockIdx.x * 256 + threadIdx.x;
+    if (e >= nel) return;
+    const T *qe = q + e * NP;
+    T *te = tau + e * NP;
+    T last_q = qe[0], last_t = (T)(6.0814 * pow((double)last_q, -1.015));
+    for (int p = 0; p < NP; ++p) {
+        const T x = qe[p];
+        if (x != last_q) {
+            last_q = x;
+            last_t = (T)(6.0814 * pow((double)x, -1.015));
+        }
+        te[p] = last_t;
+    }
 }
 
 // Min, max and a non-finite flag of v (float32 keys), reduced per block
@@ -1191,8 +1206,8 @@ int set_model_impl(sesnt_t *h, const float *rhoinv, const float *lambda, const f
     if (!rc && h->sls) {
         rc = import(q, h->tau);  // q imported in place, then mapped to tau
         if (!rc) {
-            k_tau<T><<<(unsigned)((nloc + 255) / 256), 256, 0, h->stream>>>((const T *)h->tau, (T *)h->tau,
-                                                                            (long long)nloc);
+            k_tau<T><<<(unsigned)((h->nel + 255) / 256), 256, 0, h->stream>>>((const T *)h->tau, (T *)h->tau,
+                                                                              (long long)h->nel, h->NP);
         }
     }
     if (!rc) {

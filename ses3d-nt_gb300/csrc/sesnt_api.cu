@@ -1252,38 +1252,44 @@ template <typename T>
 int v_ptp_impl(sesnt_t *h, int sim, float out[2]) {
     int rc;
     // per call: reduce and copy back on the handle's stream, one
-    // synchronisation; the words live in the handle
-    if (!h->h_ptp) {
-        void *hm = nullptr, *hd = nullptr;
-        if (cudaHostAlloc(&hm, 3 * sizeof(unsigned long long), cudaHostAllocMapped) != cudaSuccess ||
-            cudaHostGetDevicePointer(&hd, hm, 0) != cudaSuccess) {
-            if (hm) cudaFreeHost(hm);
-            cudaGetLastError();
-            return h->fail(SESNT_ENOMEM, "mapped host words for v_ptp");
-        }
-        h->h_ptp = (unsigned long long *)hm;
-        h->h_ptp_dev = (unsigned long long *)hd;
-    }
+    // synchronisation; the words live in the handle. d_ptp: [0..3] the
+    // reduction words, [4..6] the result where mapped host memory is not had.
     if (!h->d_ptp) {
-        if ((rc = h->alloc((void **)&h->d_ptp, 4 * sizeof(unsigned long long), "ptp"))) return rc;
+        if ((rc = h->alloc((void **)&h->d_ptp, 8 * sizeof(unsigned long long), "ptp"))) return rc;
         const unsigned long long init[4] = {~0ULL, 0ULL, 0ULL, 0ULL};
         cudaError_t e = cudaMemcpy(h->d_ptp, init, sizeof init, cudaMemcpyHostToDevice);
         if (e != cudaSuccess) return h->cuda_fail(e, "v_ptp");
+        void *hm = nullptr, *hd = nullptr;
+        if (h->h_ptp) {
+            // kept from an earlier call
+        } else if (cudaHostAlloc(&hm, 3 * sizeof(unsigned long long), cudaHostAllocMapped) == cudaSuccess &&
+                   cudaHostGetDevicePointer(&hd, hm, 0) == cudaSuccess) {
+            h->h_ptp = (unsigned long long *)hm;
+            h->h_ptp_dev = (unsigned long long *)hd;
+        } else {
+            if (hm) cudaFreeHost(hm);
+            cudaGetLastError();  // results come back by copy
+        }
     }
     // 8 blocks of 256 threads per SM, each thread 4 loads in flight
     k_minmax<T><<<8 * 152, 256, 0, h->stream>>>((const T *)h->v + (size_t)sim * 3 * h->nuni, 3 * h->nuni, h->d_ptp,
-                                                h->h_ptp_dev);
+                                                h->h_ptp ? h->h_ptp_dev : h->d_ptp + 4);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    unsigned long long res[3];
+    if (e == cudaSuccess) {
+        if (h->h_ptp) std::memcpy(res, h->h_ptp, sizeof res);
+        else e = cudaMemcpy(res, h->d_ptp + 4, sizeof res, cudaMemcpyDeviceToHost);
+    }
     if (e != cudaSuccess) {
         // the words may be left mid-reduction: set them up again next call
         h->release(h->d_ptp);
         h->d_ptp = nullptr;
         return h->cuda_fail(e, "v_ptp");
     }
-    out[0] = unkey(h->h_ptp[0]);
-    out[1] = unkey(h->h_ptp[1]);
-    if (h->h_ptp[2]) return h->fail(SESNT_ENONFINITE, "wavefield of simulation %d contains NaN or Inf", sim);
+    out[0] = unkey(res[0]);
+    out[1] = unkey(res[1]);
+    if (res[2]) return h->fail(SESNT_ENONFINITE, "wavefield of simulation %d contains NaN or Inf", sim);
     return SESNT_OK;
 }
 

@@ -248,10 +248,11 @@ __global__ void __launch_bounds__(TmaCfg<N, T, NSLS>::NT, TmaCfg<N, T, NSLS>::MI
 
 // One element per block with its stress and memory variables staged by bulk
 // copy (k_element_stage), the default SLS step for degrees with one element
-// per block (4-7): thread 0 starts the two copies (one contiguous chunk
-// each) before the velocity gather, so they travel during the gather, the
-// staging barrier and the line contractions, and the state costs no
-// per-thread load instructions or registers. The updated state goes back
+// per block (4-7): thread 0 starts the copy of the element's state unit
+// (stress and memory variables, one contiguous range, in 8 KB pieces)
+// before the velocity gather, so it travels during the gather, the staging
+// barrier and the line contractions, and the state costs no per-thread load
+// instructions or registers. The updated state goes back
 // into the stage and out by bulk store (STORE), or for degree 6 from
 // registers as in k_element. Measured on 3-SLS FP32 grids of 6-7 M points
 // against k_element: 3.2/4.1/10.1/10.8% faster for degrees 4/5/6/7 (degree

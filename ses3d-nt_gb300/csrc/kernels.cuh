@@ -52,7 +52,8 @@ namespace sesnt {
 #define SESNT_MINB_384 3
 #endif
 // Where k_element loads the SLS memory variables: with the other loads at
-// the start (0) or after the line contractions, still before any store (1).
+// the start (0) or right after the barrier that stages the velocities,
+// before the line contractions and any store (1).
 // -1 picks by degree: late up to degree 5, early for 6 and 7. Measured on
 // 3-SLS FP32 grids of 6-12 M points: late is 4.3/1.2/3.9/5.0% faster for
 // degrees 2/3/4/5 and 1.4/2.4% slower for 6/7; FP64 (degree 4) unchanged.

@@ -146,8 +146,9 @@ __global__ void k_tau(const T *q, T *tau, long long nel, int NP) {
 // (shuffles, then shared memory) so that each block makes one atomic per
 // word; four independent loads per iteration keep memory busy. The last
 // block to finish (counted in mm[3] after a fence) copies the result to
-// `out` (mapped host memory) and resets mm for the next call, so a call is
-// one launch and one synchronisation. No block waits for another.
+// `out` (mapped host memory, or device memory where that is not had) and
+// resets mm for the next call, so a call is one launch and one
+// synchronisation. No block waits for another.
 // mm: [0] ordered bits of the minimum, [1] of the maximum, [2] non-finite
 // flag, [3] finished blocks; all four start at {~0, 0, 0, 0}. out: the
 // three result words.

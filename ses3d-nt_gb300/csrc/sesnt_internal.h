@@ -130,6 +130,19 @@ struct StateLayout {
     static constexpr int CS = state_cs(NP, NSLS > 0);  // component stride
     static constexpr size_t UNIT = state_unit(NP, NSLS);  // values per unit
 };
+// Every unit is a legal bulk copy (the bulk-copy kernels move whole units
+// only): its size is a multiple of 16 bytes for degrees 2-7 in FP32 and FP64,
+// so every unit of an allocation starts on a 16-byte boundary.
+constexpr bool state_layout_aligned(int lpd) {
+    const int np = (lpd + 1) * (lpd + 1) * (lpd + 1);
+    for (int nsls : {0, 3})
+        for (int e : {4, 8})
+            if ((state_unit(np, nsls) * e) % 16 != 0) return false;
+    return true;
+}
+static_assert(state_layout_aligned(2) && state_layout_aligned(3) && state_layout_aligned(4) &&
+                  state_layout_aligned(5) && state_layout_aligned(6) && state_layout_aligned(7),
+              "state units must be multiples of 16 bytes");
 
 // Displacement-gradient components (src/evolution.f90:179-187).
 enum { kDuXX = 0, kDuYY, kDuZZ, kDuXY, kDuYX, kDuXZ, kDuZX, kDuYZ, kDuZY };

@@ -26,7 +26,6 @@ rank 0 prints the aggregate.
 import argparse
 import copy
 import json
-import math
 import os
 import shutil
 import statistics
@@ -237,6 +236,20 @@ def element_kernel_name(element, g):
     return "k_element"
 
 
+def graph_launches(K, per_step):
+    """Kernels a run of K steps launches: per_step per step, the step-counter
+    set at the start, and one counter advance per replayed graph that ends
+    before the run does (runs of 32 steps, then graphs of 16, 8, 4 and 2, the
+    last single step without an advance; the rules of run_steps in
+    sesnt_api.cu)."""
+    graphs, left = K // 32, K % 32
+    for n in (16, 8, 4, 2):
+        if left >= n:
+            graphs += 1
+            left -= n
+    return int(K * per_step + 1 + graphs)
+
+
 def run_ours(args):
     import numpy as np
 
@@ -287,7 +300,7 @@ def run_ours(args):
                          % (info["algorithmic_bytes_per_step"] / 1e9),
                    "graph": not (g.flags & sesnt.FLAG_NO_GRAPH), "element_kernel": args.element,
                    "parallelism": "replicas" if WORLD > 1 else "single GPU"},
-        "gpu_launches": int(K * info["launches_per_step"] + math.ceil(K / 32.0) + 1),
+        "gpu_launches": graph_launches(K, info["launches_per_step"]),
         "clocks": clk,
         "step_alg_hbm_gbs": info["algorithmic_bytes_per_step"] * K / (ms_max / 1e3) / 1e9,
         "finite": seis_ok,
@@ -314,7 +327,9 @@ def run_ours(args):
                 traffic = None
         line["roofline"] = {"bound": "hbm", "kernel": kname, "achieved": ach, "peak": hbm,
                             "peak_source": peak_kind, "unit": "GB/s", "frac": ach / hbm,
-                            "traffic": traffic, "alg_bytes_per_launch": eb}
+                            "traffic": traffic, "alg_bytes_per_launch": eb,
+                            "traffic_source": ("stored ncu capture of this kernel and workload, "
+                                               "profiles/" + os.path.basename(tr_path)) if traffic else None}
     if args.e2e and RANK == 0:
         line["e2e"] = e2e(args, wl)
     if args.accuracy_steps > 0 and RANK == 0:

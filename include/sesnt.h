@@ -11,7 +11,7 @@
  *   - point location / Vandermonde      src/config/point.f90:150-254
  * called from the forward loop at src/ses3d-nt.F90:240-270.
  * This header replaces them with explicit, handle-based entry points that a
- * Fortran driver binds through ISO_C_BINDING (see INTEGRATION.md).
+ * Fortran driver binds through ISO_C_BINDING.
  *
  * Conventions
  *   - Every function returns SESNT_OK (0) or a negative SESNT_E* code; the
@@ -309,6 +309,15 @@ int sesnt_get_field(sesnt_t *h, int sim, int which, void *out, int out_precision
  * whose result arrives in mapped host memory. */
 int sesnt_v_ptp(sesnt_t *h, int sim, float out[2]);
 
+/* Kinetic energy of simulation `sim`, the reference's kinetic_energy
+ * (src/elastic_vars.F90:218-246): 0.5 * jac * sum over element-local points
+ * of (vx^2 + vy^2 + vz^2) * r^2 sin(theta) * rho * w_i w_j w_k, in joules.
+ * Computed on the device in FP64 from the unique-point velocity and the
+ * assembled mass (every copy of a shared point holds the same velocity), with
+ * a fixed summation order, so repeated calls give identical results.
+ * SESNT_ENONFINITE if the result is NaN or Inf. Synchronous. */
+int sesnt_kinetic_energy(sesnt_t *h, int sim, double *out);
+
 /* Sums an element-local field over every copy of each shared GLL point and
  * writes the sum back to every copy: the effect of
  * communicate_local_boundaries (src/communicate_fields.F90:48-79) on one
@@ -316,18 +325,21 @@ int sesnt_v_ptp(sesnt_t *h, int sim, float out[2]);
  * field is float32 in the reference raw layout; in place. Synchronous. */
 int sesnt_assemble_field(sesnt_t *h, float *field);
 
-/* No counterpart in the reference. The same assembly as
- * sesnt_assemble_field, for callers that cannot allocate device memory at the
- * time of the call (a time loop that must not synchronise the whole device
- * as cudaMalloc/cudaFree may, a host that reserved all device memory up
- * front). d_in and d_out are device
+/* No counterpart in the reference. The assembly of sesnt_assemble_field, for
+ * callers that cannot allocate device memory at the time of the call (a time
+ * loop that must not synchronise the whole device as cudaMalloc/cudaFree may,
+ * a host that reserved all device memory up front). d_in and d_out are device
  * pointers to float32 fields in the reference raw layout and may be the same
  * buffer. Nothing is allocated: the unique-point sums use a fixed device
  * array of 4,194,304 floats (16 MiB) that every GPU loading this library
- * holds until exit; grids with more unique points get SESNT_ERANGE. The first
- * call on a device looks up that array's address, so make it before any
- * stream capture. All calls share the array: calls that overlap on the GPU
- * race. Runs on the handle's stream and waits for it. */
+ * holds until exit; grids with more unique points get SESNT_ERANGE. The sums
+ * are float32 whatever the handle's precision (sesnt_assemble_field sums an
+ * FP64 handle's field in float64), so on FP64 handles the two can differ by
+ * float32 rounding. The first call on a device looks up that array's address
+ * (a set-up step): make that first call before any stream capture. All calls
+ * share the array: calls that overlap on the GPU race. The calling thread's
+ * current device must be the handle's (SESNT_EINVAL otherwise). Runs on the
+ * handle's stream and synchronises that stream before it returns. */
 int sesnt_assemble_field_noalloc(sesnt_t *h, const float *d_in, float *d_out);
 
 /* Sizes: out[0] elements, out[1] element-local GLL points (N_loc), out[2]

@@ -314,7 +314,7 @@ struct Sim {
     std::vector<T> dl;  // dl[i*P+j] = get_dlgll(N,i,j)
     std::vector<T> x1, y1, z1;  // 1-D coordinates [e*P+n]
     std::vector<T> r, sin_t, cot_t, r_sin, rr_sin, W, taper;
-    std::vector<T> lambda, mu, rhoinv, A, B, C, qq, two_mu, kappa, tau, mu_tau, MM;
+    std::vector<T> lambda, mu, rhoinv, A, B, C, qq, two_mu, kappa, tau, mu_tau, MM, rho;
     bool visco = false;
     static constexpr int nrdiss = 3;
     T tau_p[3] = {T(1000.00), T(70.00), T(5.25)};  // src/geometric_paras.f90:41-42
@@ -422,7 +422,7 @@ struct Sim {
     // init_auxiliary_model_parameters: src/model_paras.F90:389-416.
     void init_aux() {
         two_mu.resize(nloc); kappa.resize(nloc); tau.resize(nloc); mu_tau.resize(nloc); MM.resize(nloc);
-        std::vector<T> rho(nloc);
+        rho.assign(nloc, T(0));
         visco = false;
         for (size_t a = 0; a < nloc; ++a)
             if (qq[a] != std::numeric_limits<T>::max()) visco = true;  // src/evolution.f90:70-74
@@ -435,6 +435,16 @@ struct Sim {
             MM[a] = -(jac * (r[a] * r[a]) * sin_t[a] * rho[a] * W[a]);
         }
         assemble_local(MM.data(), nx, ny, nz, N);
+    }
+
+    // kinetic_energy: src/elastic_vars.F90:218-246, the element-local sum in
+    // the working precision, Fortran array order (one rank: the MPI_ALLREDUCE
+    // sum is the identity).
+    T kinetic_energy() const {
+        T s = T(0);
+        for (size_t a = 0; a < nloc; ++a)
+            s += (vx[a] * vx[a] + vy[a] * vy[a] + vz[a] * vz[a]) * rr_sin[a] * rho[a] * W[a];
+        return T(0.5) * jac * s;
     }
 
     void alloc_state() {
@@ -1057,6 +1067,12 @@ int oracle_courant(void *hv, float out[2]) {
     } else {
         S<float>(h)->courant(out);
     }
+    return 0;
+}
+
+int oracle_kinetic_energy(void *hv, double *out) {
+    Handle *h = (Handle *)hv;
+    *out = h->precision == 8 ? S<double>(h)->kinetic_energy() : (double)S<float>(h)->kinetic_energy();
     return 0;
 }
 

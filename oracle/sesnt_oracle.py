@@ -65,6 +65,7 @@ def lib():
         _L.oracle_get_seismograms.argtypes = [V, V]
         _L.oracle_destroy.argtypes = [V]
         _L.oracle_is_visco.argtypes = [V]
+        _L.oracle_kinetic_energy.argtypes = [V, dp]
         _L.oracle_gll_f32.argtypes = [C.c_int, fp, fp, fp]
         _L.oracle_gll_f64.argtypes = [C.c_int, dp, dp, dp]
         _L.oracle_coordinates_1d.argtypes = [C.c_int, C.c_int, C.c_float, C.c_float, fp]
@@ -218,6 +219,12 @@ class Oracle:
 
     def visco(self):
         return bool(lib().oracle_is_visco(self._h))
+
+    def kinetic_energy(self):
+        """kinetic_energy of src/elastic_vars.F90:218-246 in the oracle's precision."""
+        out = C.c_double(0.0)
+        lib().oracle_kinetic_energy(self._h, C.byref(out))
+        return out.value
 
 
 def load_workload(o, wl, sim=0, masks=None):

@@ -9,7 +9,7 @@
 // holds that array until the process exits. All calls share it: the array
 // keeps the previous call's sums, so each call clears the part it uses, and
 // calls whose work overlaps on the GPU (different handles or streams at the
-// same time) race on it.
+// same time) race on it. The sums are float32 for every handle precision.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -27,11 +27,10 @@ constexpr int kMaxDevices = 64;
 std::mutex g_setup_mutex;
 float *g_unique_ptr[kMaxDevices] = {};
 
-// Device address of the accumulator for the current device, looked up once
-// per device (with that device current) and cached.
-int unique_scratch(float **out) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return -1;
+// Device address of the accumulator on device `dev` (the current device),
+// looked up once per device with that device current and cached.
+int unique_scratch(int dev, float **out) {
+    if (dev < 0 || dev >= kMaxDevices) return -1;
     std::lock_guard<std::mutex> lock(g_setup_mutex);
     if (!g_unique_ptr[dev]) {
         void *p = nullptr;
@@ -92,8 +91,18 @@ extern "C" int sesnt_assemble_field_noalloc(sesnt_t *h, const float *d_in, float
                                   "sesnt_assemble_field_noalloc: grid has %lld unique points, the fixed scratch "
                                   "holds at most %lld; use sesnt_assemble_field",
                                   g.nuni, kNoAllocMaxUnique);
+    // the handle's stream and the array's address belong to the handle's device
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess)
+        return sesnt::handle_fail(h, SESNT_ECUDA, "sesnt_assemble_field_noalloc: cudaGetDevice failed: %s",
+                                  cudaGetErrorString(cudaGetLastError()));
+    if (dev != sesnt::handle_device(h))
+        return sesnt::handle_fail(h, SESNT_EINVAL,
+                                  "sesnt_assemble_field_noalloc: the current device is %d but the handle was "
+                                  "created on device %d; make the handle's device current first",
+                                  dev, sesnt::handle_device(h));
     float *uni = nullptr;
-    if (unique_scratch(&uni))
+    if (unique_scratch(dev, &uni))
         return sesnt::handle_fail(h, SESNT_ECUDA, "sesnt_assemble_field_noalloc: cudaGetSymbolAddress failed: %s",
                                   cudaGetErrorString(cudaGetLastError()));
     cudaStream_t st = (cudaStream_t)sesnt_stream(h);
@@ -101,8 +110,10 @@ extern "C" int sesnt_assemble_field_noalloc(sesnt_t *h, const float *d_in, float
     k_zero<<<bu, 256, 0, st>>>(uni, g.nuni);  // the array keeps the previous call's sums
     k_scatter_raw<<<bl, 256, 0, st>>>(g, d_in, uni);
     k_gather_raw<<<bl, 256, 0, st>>>(g, uni, d_out);
-    cudaError_t e = cudaStreamSynchronize(st);
-    if (e == cudaSuccess) e = cudaGetLastError();
+    // launch errors of these three kernels, before the synchronisation can
+    // report (and clear) an error left by unrelated earlier work
+    cudaError_t e = cudaPeekAtLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess)
         return sesnt::handle_fail(h, SESNT_ECUDA, "sesnt_assemble_field_noalloc: %s", cudaGetErrorString(e));
     return SESNT_OK;

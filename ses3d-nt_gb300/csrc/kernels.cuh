@@ -293,14 +293,21 @@ __device__ __forceinline__ void point_update(const StepArgs<T> &a, const T (&e)[
     put(sig + 5 * cs, szz * tp);
     if constexpr (NSLS > 0) {
         // memory variables after the update, driven by this step's rates:
-        // M <- M*(1 - dt/tau_p) - tau*dt/(n*tau_p)*e
+        // M <- M - M*(dt/tau_p) - tau*dt/(n*tau_p)*e, the reference's form
+        // (src/evolution.f90:415-442). Folding the decay into one factor
+        // (1 - dt/tau_p) rounds that factor near 1 and biases the decay rate
+        // of every step the same way: by 6.3e-4 of dt/tau_p for tau_p =
+        // 1000 s and dt = 0.03 s. Kept apart, the rate dt/tau_p is rounded
+        // to 2^-24 of itself.
         const T er[6] = {exx, eyy, ezz, exy, exz, eyz};
 #pragma unroll
         for (int q = 0; q < NSLS; ++q) {
             const T drive = tau * a.mem_drive[q];
 #pragma unroll
-            for (int c = 0; c < 6; ++c)
-                put(mem + (size_t)(c * NSLS + q) * cs, m[c][q] * a.mem_keep[q] - drive * er[c]);
+            for (int c = 0; c < 6; ++c) {
+                const T mo = m[c][q];
+                put(mem + (size_t)(c * NSLS + q) * cs, (mo - mo * a.mem_rate[q]) - drive * er[c]);
+            }
         }
     }
     // metric-weighted stresses for the weak divergence

@@ -215,6 +215,34 @@ __global__ void __launch_bounds__(256) k_minmax(const T *v, long long n, unsigne
     }
 }
 
+// Kinetic energy of one simulation, 0.5*jac*sum over element-local points of
+// |v|^2 * r^2 sin(theta) * rho * w_i w_j w_k (src/elastic_vars.F90:218-246).
+// Every copy of a shared point carries the same v, and the assembled mass of
+// a unique point is the sum of -jac*r^2 sin(theta)*rho*w_i w_j w_k over its
+// copies (src/model_paras.F90:410-415), so the sum is -0.5 * sum over unique
+// points of |v|^2 / invM: one pass over v and 1/M. Each block sums in FP64
+// in a fixed order and writes its partial; the host adds the partials in
+// block order, so the result is the same on every call.
+template <typename T>
+__global__ void __launch_bounds__(256) k_kinetic(const T *__restrict__ v, const T *__restrict__ invM, long long nuni,
+                                                 double *__restrict__ partial) {
+    double acc = 0.0;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long u = (long long)blockIdx.x * blockDim.x + threadIdx.x; u < nuni; u += stride) {
+        const double x = (double)v[u], y = (double)v[nuni + u], z = (double)v[2 * nuni + u];
+        acc += (x * x + y * y + z * z) / (double)invM[u];
+    }
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    __shared__ double sw[8];
+    if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) b += sw[q];
+        partial[blockIdx.x] = -0.5 * b;
+    }
+}
+
 float unkey(unsigned long long k) {
     unsigned b = (unsigned)k;
     b = (b & 0x80000000u) ? (b & 0x7fffffffu) : ~b;
@@ -319,8 +347,16 @@ struct sesnt_handle {
     cudaGraphExec_t graph = nullptr;
     int graph_steps = 0;
     cudaGraphExec_t graph1 = nullptr;  // one step, for sesnt_step
+    // graphs of 16, 8, 4 and 2 steps that advance the step counter, for the
+    // remainder of a run below kGraphSteps (index log2(steps) - 1), built
+    // when a run first needs them
+    static constexpr int kLadder = 4;
+    cudaGraphExec_t ladder[kLadder] = {};
     // v_ptp: device reduction words and the mapped host words of the result
     unsigned long long *d_ptp = nullptr, *h_ptp = nullptr, *h_ptp_dev = nullptr;
+    // kinetic energy: per-block partial sums (kinetic_blocks doubles)
+    double *d_kin = nullptr;
+    int sms = 0;  // multiprocessors of the handle's device (grid sizes of the reductions)
 
     // events for timing
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -400,6 +436,10 @@ struct sesnt_handle {
         graph_steps = 0;
         if (graph1) cudaGraphExecDestroy(graph1);
         graph1 = nullptr;
+        for (cudaGraphExec_t &l : ladder) {
+            if (l) cudaGraphExecDestroy(l);
+            l = nullptr;
+        }
     }
     void free_seis_mirror() {
         if (h_seis) cudaFreeHost(h_seis);
@@ -433,7 +473,7 @@ struct sesnt_handle {
         a.inv_alpha = alpha > 0 ? (T)(1.0 / alpha) : T(0);
         for (int q = 0; q < kNsls; ++q) {
             a.tau_p[q] = (T)kTauP[q];
-            a.mem_keep[q] = (T)(1.0 - dt / kTauP[q]);
+            a.mem_rate[q] = (T)(dt / kTauP[q]);
             a.mem_drive[q] = (T)(dt / (kNsls * kTauP[q]));
         }
         a.inv_r = (const T *)inv_r; a.inv_sin = (const T *)inv_sin;
@@ -468,6 +508,7 @@ struct sesnt_handle {
 
 namespace sesnt {
 const sesnt_grid *handle_grid(const sesnt_handle *h) { return &h->g; }
+int handle_device(const sesnt_handle *h) { return h->device; }
 int handle_fail(sesnt_handle *h, int code, const char *fmt, ...) {
     char buf[512];
     va_list ap;
@@ -886,15 +927,17 @@ int enqueue_steps(sesnt_t *h, int n, bool rot_full = false) {
 
 constexpr int kGraphSteps = 32;
 
-// Captures n steps (n = kGraphSteps: advancing the step counter by n at the
-// end; n = 1: the step at the counter, for sesnt_step) into *exec.
+// Captures n steps starting at the step counter into *exec; with `advance`
+// the graph ends by advancing the counter by n (graphs replayed back to back
+// within one run), without it the counter is left as it was (the one-step
+// graph of sesnt_step, whose run sets the counter first).
 template <typename T>
-int capture_steps(sesnt_t *h, int n, cudaGraphExec_t *exec) {
+int capture_steps(sesnt_t *h, int n, cudaGraphExec_t *exec, bool advance) {
     cudaGraph_t gr = nullptr;
     cudaError_t e = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return h->cuda_fail(e, "cudaStreamBeginCapture");
     int rc = enqueue_steps<T>(h, n);
-    if (!rc && n > 1) k_advance_it<<<1, 1, 0, h->stream>>>(h->d_it, n);
+    if (!rc && advance) k_advance_it<<<1, 1, 0, h->stream>>>(h->d_it, n);
     e = cudaStreamEndCapture(h->stream, &gr);
     if (rc) {
         if (gr) cudaGraphDestroy(gr);
@@ -912,14 +955,18 @@ int capture_steps(sesnt_t *h, int n, cudaGraphExec_t *exec) {
 
 template <typename T>
 int build_graph(sesnt_t *h) {
-    h->drop_graph();
-    int rc = capture_steps<T>(h, kGraphSteps, &h->graph);
+    int rc = capture_steps<T>(h, kGraphSteps, &h->graph, true);
     if (rc) return rc;
     h->graph_steps = kGraphSteps;
     return SESNT_OK;
 }
 
-// Steps it0 .. it0+nsteps-1 (prepared): graph replays and direct launches.
+// Steps it0 .. it0+nsteps-1 (prepared): graph replays (runs of kGraphSteps,
+// then the remainder as graphs of 16, 8, 4, 2 and 1 steps, so a short run
+// costs at most five graph launches), or direct launches without graphs.
+// A run of 2..31 steps launched directly measured about 15 us per step slower
+// than replayed (config 2: 0.302 against 0.287 ms): the per-step stream
+// fork and join cost more as launches than as graph edges.
 template <typename T>
 int run_steps(sesnt_t *h, int it0, int nsteps) {
     int rc;
@@ -934,9 +981,19 @@ int run_steps(sesnt_t *h, int it0, int nsteps) {
             h->mark(it0 + nsteps - left - 1);
         }
     }
+    for (int q = sesnt_handle::kLadder - 1; h->use_graph && q >= 0; --q) {
+        const int n = 2 << q;  // 16, 8, 4, 2
+        if (left < n) continue;
+        if (!h->ladder[q] && (rc = capture_steps<T>(h, n, &h->ladder[q], true))) return rc;
+        cudaError_t e = cudaGraphLaunch(h->ladder[q], h->stream);
+        if (e != cudaSuccess) return h->cuda_fail(e, "cudaGraphLaunch");
+        left -= n;
+        h->mark(it0 + nsteps - left - 1);
+    }
     if (left == 1 && h->use_graph) {
-        // a single step (the sesnt_step loop of a driver): one graph launch
-        if (!h->graph1 && (rc = capture_steps<T>(h, 1, &h->graph1))) return rc;
+        // a single step (the last of a run, or the sesnt_step loop of a
+        // driver): one graph launch
+        if (!h->graph1 && (rc = capture_steps<T>(h, 1, &h->graph1, false))) return rc;
         cudaError_t e = cudaGraphLaunch(h->graph1, h->stream);
         if (e != cudaSuccess) return h->cuda_fail(e, "cudaGraphLaunch");
         h->mark(it0 + nsteps - 1);
@@ -1273,7 +1330,7 @@ int v_ptp_impl(sesnt_t *h, int sim, float out[2]) {
         }
     }
     // 8 blocks of 256 threads per SM, each thread 4 loads in flight
-    k_minmax<T><<<8 * 152, 256, 0, h->stream>>>((const T *)h->v + (size_t)sim * 3 * h->nuni, 3 * h->nuni, h->d_ptp,
+    k_minmax<T><<<8 * h->sms, 256, 0, h->stream>>>((const T *)h->v + (size_t)sim * 3 * h->nuni, 3 * h->nuni, h->d_ptp,
                                                 h->h_ptp ? h->h_ptp_dev : h->d_ptp + 4);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
@@ -1291,6 +1348,27 @@ int v_ptp_impl(sesnt_t *h, int sim, float out[2]) {
     out[0] = unkey(res[0]);
     out[1] = unkey(res[1]);
     if (res[2]) return h->fail(SESNT_ENONFINITE, "wavefield of simulation %d contains NaN or Inf", sim);
+    return SESNT_OK;
+}
+
+template <typename T>
+int kinetic_impl(sesnt_t *h, int sim, double *out) {
+    const int blocks = 4 * h->sms;  // 4 blocks of 256 threads per SM
+    int rc;
+    if (!h->d_kin && (rc = h->alloc((void **)&h->d_kin, (size_t)blocks * sizeof(double), "kinetic energy")))
+        return rc;
+    k_kinetic<T><<<blocks, 256, 0, h->stream>>>((const T *)h->v + (size_t)sim * 3 * h->nuni, (const T *)h->invM,
+                                                h->nuni, h->d_kin);
+    cudaError_t e = cudaPeekAtLastError();
+    std::vector<double> part(blocks);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(part.data(), h->d_kin, part.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return h->cuda_fail(e, "kinetic_energy");
+    double sum = 0.0;
+    for (double x : part) sum += x;
+    *out = sum;
+    if (!std::isfinite(sum)) return h->fail(SESNT_ENONFINITE, "wavefield of simulation %d contains NaN or Inf", sim);
     return SESNT_OK;
 }
 
@@ -1372,6 +1450,10 @@ int sesnt_create(const sesnt_grid_t *grid, sesnt_t **out) {
     h->use_graph = (grid->flags & SESNT_FLAG_NO_GRAPH) == 0;
     h->launches_per_step = 4;
     cudaGetDevice(&h->device);
+    if (cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess || h->sms <= 0) {
+        cudaGetLastError();
+        h->sms = 152;
+    }
     cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -1753,6 +1835,14 @@ int sesnt_v_ptp(sesnt_t *h, int sim, float out[2]) {
     if (!h || !out) return SESNT_EINVAL;
     if (sim < 0 || sim >= h->S) return h->fail(SESNT_ERANGE, "simulation %d outside 0..%d", sim, h->S - 1);
     return h->dbl ? v_ptp_impl<double>(h, sim, out) : v_ptp_impl<float>(h, sim, out);
+}
+
+int sesnt_kinetic_energy(sesnt_t *h, int sim, double *out) {
+    Range r("sesnt_kinetic_energy");
+    if (!h || !out) return SESNT_EINVAL;
+    if (sim < 0 || sim >= h->S) return h->fail(SESNT_ERANGE, "simulation %d outside 0..%d", sim, h->S - 1);
+    if (!h->model_set) return h->fail(SESNT_ESTATE, "sesnt_set_model must be called before sesnt_kinetic_energy");
+    return h->dbl ? kinetic_impl<double>(h, sim, out) : kinetic_impl<float>(h, sim, out);
 }
 
 int sesnt_assemble_field(sesnt_t *h, float *field) {

@@ -27,6 +27,7 @@ namespace sesnt {
 
 // Handle accessors for entry points defined outside sesnt_api.cu.
 const sesnt_grid *handle_grid(const sesnt_handle *h);
+int handle_device(const sesnt_handle *h);  // the device current at sesnt_create
 int handle_fail(sesnt_handle *h, int code, const char *fmt, ...);
 
 constexpr int kMaxLpd = 7;
@@ -54,7 +55,7 @@ struct StepArgs {
     long long nuni, nloc;
     T dt, c1, c2, c3, jac, alpha, inv_alpha;
     T tau_p[kNsls];
-    T mem_keep[kNsls];   // 1 - dt/tau_p(k)
+    T mem_rate[kNsls];   // dt/tau_p(k)
     T mem_drive[kNsls];  // dt/(n_sls*tau_p(k))
     // small tables (device): tabD = [Dx | Dy | Dz | Dt], each P*P
     const T *tabD, *w, *sin_t, *cot_t, *r, *px, *py, *pz;

@@ -159,6 +159,7 @@ def lib():
         "sesnt_get_seismograms": (I, [P, fp]),
         "sesnt_get_field": (I, [P, I, I, P, I]),
         "sesnt_v_ptp": (I, [P, I, fp]),
+        "sesnt_kinetic_energy": (I, [P, I, C.POINTER(C.c_double)]),
         "sesnt_assemble_field": (I, [P, fp]),
         "sesnt_info": (I, [P, C.POINTER(C.c_longlong)]),
         "sesnt_footprint_bytes": (C.c_longlong, [G]),
@@ -371,6 +372,12 @@ class Simulation:
         out = np.zeros(2, np.float32)
         self._c(lib().sesnt_v_ptp(self._h, sim, _fptr(out)))
         return float(out[0]), float(out[1])
+
+    def kinetic_energy(self, sim=0):
+        """Kinetic energy of simulation `sim` in joules (elastic_vars.F90:218-246)."""
+        out = C.c_double(0.0)
+        self._c(lib().sesnt_kinetic_energy(self._h, sim, C.byref(out)))
+        return out.value
 
     def assemble(self, field):
         f = _f32(field, self.grid.n_loc).copy()

@@ -3,8 +3,8 @@ the reference's own Python reader (ses3dpy.namelist.namelist2dict).
 
 The reader is Python 2 code; importing it here under Python 3 needs only the
 old StringIO module name, which is supplied from io. Run from the repository
-root with the reference checked out at /root/reference:
-    python tests/golden/make_config_golden.py
+root with SES3D_NT_REFERENCE naming a checkout of the reference:
+    SES3D_NT_REFERENCE=path/to/Ses3d-NT python tests/golden/make_config_golden.py
 """
 import glob
 import io
@@ -13,10 +13,12 @@ import os
 import sys
 import types
 
-REFERENCE = os.environ.get("SES3D_NT_REFERENCE", "/root/reference")
+REFERENCE = os.environ.get("SES3D_NT_REFERENCE", "")
 
 
 def reference_reader():
+    if not REFERENCE or not os.path.isdir(os.path.join(REFERENCE, "ses3dpy")):
+        raise SystemExit("set SES3D_NT_REFERENCE to a checkout of the reference (it holds ses3dpy/)")
     m = types.ModuleType("StringIO")
     m.StringIO = io.StringIO
     sys.modules.setdefault("StringIO", m)

@@ -55,6 +55,32 @@ def test_noalloc_assembly_matches_allocating_entry_point(gpu, sesnt_lib):
             assert np.array_equal(d.cpu().numpy().reshape(g.shape, order="F"), sim.assemble(f))
 
 
+def test_noalloc_on_an_fp64_handle_sums_in_float32(gpu, sesnt_lib):
+    """On an FP64 handle the allocating entry point sums in float64 and the
+    no-allocation one in float32: with non-integer data they agree to float32
+    rounding of sums of up to 8 copies of values in [-1, 1]: at most 7
+    float32 additions per point, each rounding by at most 2^-24 of a partial
+    sum below 8, i.e. 3.4e-6 absolute; the test bounds the difference by 2e-6
+    of the largest sum (about 5 on this grid)."""
+    torch = pytest.importorskip("torch")
+    g = _grid(lpd=5)
+    g.precision = 8
+    with sesnt.Simulation(g) as sim:
+        rng = np.random.default_rng(31)
+        for call in range(2):
+            f = np.asfortranarray(rng.uniform(-1.0, 1.0, size=g.shape).astype(np.float32))
+            want = sim.assemble(f)
+            d_in = torch.from_numpy(np.ascontiguousarray(f.ravel(order="F"))).to("cuda")
+            d_out = torch.full_like(d_in, float("nan"))
+            torch.cuda.synchronize()
+            assert _noalloc(sim, d_in, d_out) == sesnt.OK, sesnt.lib().sesnt_last_error(sim.handle)
+            got = d_out.cpu().numpy().reshape(g.shape, order="F")
+            err = float(np.abs(got.astype(np.float64) - want).max() / np.abs(want).max())
+            print("FP64 handle, call %d: no-allocation vs allocating assembly %.2e of the largest sum"
+                  % (call, err))
+            assert err < 2e-6, call
+
+
 def test_noalloc_rejects_grids_beyond_the_fixed_scratch(gpu, sesnt_lib):
     torch = pytest.importorskip("torch")
     g = _grid(nx=64, ny=64, nz=16, lpd=4)  # 257*257*65 = 4.29M unique points > 4,194,304

@@ -222,9 +222,12 @@ def cpu_oracle_rate(wl, budget_s, max_steps=None, warm=2):
 # arms
 # ---------------------------------------------------------------------------
 def element_kernel_name(element, g):
-    """The element kernel the library launches for this grid and --element
-    choice (the launch rules of kernels.cuh:launch_element)."""
+    """The element kernel the library's launch rules pick for this grid and an
+    --element choice other than tuned/columns (kernels.cuh:plan_element); a
+    run reads the kernel it actually launched from the library."""
     import sesnt
+    if element == "columns":
+        return "k_element_cols" if g.n_sls == 0 else element_kernel_name("simple", g)
     if element.startswith("tc_"):
         return "k_element_tc"
     if element == "persistent":
@@ -267,6 +270,8 @@ def run_ours(args):
 
     sim = sesnt.Simulation(g)
     workloads.setup(sim, wl)
+    tune_report = choose_element(sim, args.element)
+    kname, choice = sim.element_kernel()
     info = sim.info()
     aniso = False
     if W > 0:
@@ -298,7 +303,9 @@ def run_ours(args):
                    "algorithmic_bytes_per_step": info["algorithmic_bytes_per_step"],
                    "l2": "inputs larger than L2 (%.2f GB touched per step vs 0.13 GB L2)"
                          % (info["algorithmic_bytes_per_step"] / 1e9),
-                   "graph": not (g.flags & sesnt.FLAG_NO_GRAPH), "element_kernel": args.element,
+                   "graph": not (g.flags & sesnt.FLAG_NO_GRAPH), "element": args.element,
+                   "element_kernel": {"name": kname, "variant": choice[0], "arg": choice[1], "piece": choice[2],
+                                      "tuning": tune_report.strip().splitlines()[-1] if tune_report else None},
                    "parallelism": "replicas" if WORLD > 1 else "single GPU"},
         "gpu_launches": graph_launches(K, info["launches_per_step"]),
         "clocks": clk,
@@ -312,9 +319,8 @@ def run_ours(args):
         prof = [float(x) for x in prof]
         line["kernels_ms_per_step"] = {"element": prof[0] / KP, "sources": prof[1] / KP, "node": prof[2] / KP,
                                        "receivers": prof[3] / KP}
-        kname = element_kernel_name(args.element, g)
         traffic = None
-        tr_path = os.path.join(ROOT, "profiles", "%s_%s.traffic.json" % (kname, wl.name))
+        tr_path = os.path.join(ROOT, "profiles", "%s_%s.traffic.json" % (kname.split()[0], wl.name))
         if os.path.exists(tr_path):
             try:
                 with open(tr_path) as f:
@@ -334,12 +340,98 @@ def run_ours(args):
         line["e2e"] = e2e(args, wl)
     if args.accuracy_steps > 0 and RANK == 0:
         line["accuracy_vs_fp64"] = accuracy(args, wl)
+    if args.batched and RANK == 0 and WORLD == 1 and args.workload == "config2" and not args.grid:
+        line["batched"] = batched_headline(args)
     if RANK == 0 and WORLD == 1 and args.cpu_seconds > 0:
         rate, n, el, threads = cpu_oracle_rate(wl, args.cpu_seconds)
         line["cpu_baseline"] = {"value": rate, "unit": METRIC, "cores": threads, "kind": "port",
                                 "sample": "%d time steps of the full %s grid (oracle, %d OpenMP threads, %.1f s)"
                                           % (n, wl.name, threads, el)}
     return line
+
+
+def choose_element(sim, element):
+    """Apply an --element choice that is not a grid flag: `tuned` runs the
+    library's tuner on this grid (sesnt_tune, which also caches the choice
+    for SESNT_FLAG_AUTOTUNE handles), `columns` forces the column kernel.
+    Returns the tuning report or None."""
+    import sesnt
+    if element == "tuned":
+        return sim.tune()
+    if element == "columns":
+        sim.set_element_variant(sesnt.ELEMENT_COLUMNS, 0)
+    return None
+
+
+def timed_rate(wl, K, W, KP=0, element="tuned"):
+    """Steps of one workload: W untimed, K timed with CUDA events on the
+    library's stream, then KP steps with per-kernel events. Returns
+    (GLL-point-updates/s, ms/step, info, element-kernel ms per step or None,
+    element kernel name)."""
+    import sesnt
+    import workloads
+    g = wl.grid
+    with sesnt.Simulation(g) as sim:
+        workloads.setup(sim, wl)
+        choose_element(sim, element)
+        kname = sim.element_kernel()[0]
+        info = sim.info()
+        sim.run(1, W)
+        sim.synchronize()
+        ms = sim.run_timed(W + 1, K)
+        el = float(sim.run_profiled(W + K + 1, KP)[0]) / KP if KP > 0 else None
+    return g.n_loc * K * g.batch / (ms / 1e3), ms / K, info, el, kname
+
+
+def batched_headline(args):
+    """The batched form against the plain one-source step on the same grid
+    and model: 64 simulations (one per seeded source) in one handle, whose
+    steps read the shared material, metric and mass once per element block,
+    against one simulation. Two grids: the batched workload's own (64x64x32,
+    lpd 4, 3 SLS) and the plain workload's (12x12x8, lpd 4, elastic). For
+    each: the batched and plain rates, their ratio, the batched element
+    kernel's algorithmic bytes over its event-timed duration as a fraction
+    of the measured HBM bandwidth, and the whole step's algorithmic bytes over
+    the step time as the same fraction. The target is at least 2x the plain
+    rate at at least 0.7 of HBM."""
+    import numpy as np
+    import workloads
+    hbm, peak_kind = peaks()
+    out = {"peak_gbs": hbm, "peak_source": peak_kind, "target": {"vs_plain": 2.0, "hbm_frac": 0.7}}
+    cases = (("config4_batched_64src_64x64x32_lpd4", lambda nt: workloads.config4(nt=nt), 4, 2, 3),
+             ("config1_grid_batched_64src_12x12x8_lpd4", None, 100, 5, 10))
+    for name, make, K, W, KP in cases:
+        nt = W + K + KP + 1
+        if make is None:
+            wl = workloads.config1(nt=max(nt, 400 + 16))
+            wl.grid.batch = 64
+            wl.sources = workloads.random_sources(wl.grid, 64, np.random.Generator(np.random.PCG64(1)))
+        else:
+            wl = make(nt)
+        rate, ms, info, t_el, kname = timed_rate(wl, K, W, KP)
+        plain = copy.copy(wl)
+        plain.grid = copy.copy(wl.grid)
+        plain.grid.batch = 1
+        plain.sources = [copy.copy(wl.sources[0])]
+        plain.sources[0].sim = 0
+        Kp = 400 if make is None else 40
+        plain.grid.nt = max(plain.grid.nt, 5 + Kp + 1)
+        prate, pms, pinfo, _, pname = timed_rate(plain, Kp, 5)
+        eb = element_kernel_bytes(wl.grid)
+        el_frac = eb / (t_el / 1e3) / 1e9 / hbm
+        step_frac = info["algorithmic_bytes_per_step"] / (ms / 1e3) / 1e9 / hbm
+        out[name] = {
+            "batch": wl.grid.batch, "steps": K, "warmup": W, "ms_per_step": ms, "value": rate,
+            "element_kernel": kname,
+            "plain": {"ms_per_step": pms, "value": prate, "steps": Kp, "element_kernel": pname,
+                      "l2": "inputs larger than L2" if pinfo["algorithmic_bytes_per_step"] > 129e6
+                      else "%.0f MB per step: L2-resident, as in a real run (no flush)"
+                           % (pinfo["algorithmic_bytes_per_step"] / 1e6)},
+            "vs_plain": rate / prate,
+            "element_kernel_ms": t_el, "element_kernel_hbm_frac": el_frac, "step_hbm_frac": step_frac,
+            "target_met": bool(rate / prate >= 2.0 and step_frac >= 0.7),
+        }
+    return out
 
 
 def accuracy(args, wl):
@@ -397,6 +489,12 @@ def e2e_job(args, wl):
     K = args.steps
     g = wl.grid
     model_bytes = sum(int(np.asarray(v).nbytes) for v in wl.model.values())
+    if args.element == "tuned":
+        # a user's handle: the tuner's choice comes from the tuning cache that
+        # the measured run's sesnt_tune wrote (SESNT_FLAG_AUTOTUNE)
+        g = copy.copy(g)
+        g.flags |= sesnt.FLAG_AUTOTUNE
+        wl = workloads.Workload(wl.name, g, wl.model, wl.sources, wl.receivers)
     t0 = time.perf_counter()
     sim = sesnt.Simulation(g)
     workloads.setup(sim, wl)
@@ -533,10 +631,16 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-seconds", type=float, default=60.0)
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
-    ap.add_argument("--element", default="simple",
-                    choices=["persistent", "simple", "unstaged", "tc_tf32x3", "tc_bf16x3"],
-                    help="element kernel variant (all compute the full step; tc_*: tcgen05 contractions)")
+    ap.add_argument("--no-batched", dest="batched", action="store_false",
+                    help="skip the batched-against-plain comparison of the default run")
+    ap.add_argument("--element", default="tuned",
+                    choices=["tuned", "simple", "columns", "persistent", "unstaged", "tc_tf32x3", "tc_bf16x3"],
+                    help="element kernel variant (all compute the full step): tuned = the library's tuner "
+                         "picks on this grid; simple = the launch rules; tc_*: tcgen05 contractions")
     args = ap.parse_args()
+    # the tuning cache of this run (sesnt_tune writes it, SESNT_FLAG_AUTOTUNE handles read it)
+    import tempfile
+    os.environ.setdefault("SESNT_TUNE_CACHE", os.path.join(tempfile.mkdtemp(prefix="sesnt_bench_"), "tune.txt"))
     if args.warmup < 3:
         raise SystemExit("--warmup must be >= 3")
     if args.impl == "reference":

@@ -65,6 +65,21 @@ extern "C" {
 #define SESNT_FLAG_ROTATION 64u   /* compute the rotation strain of the whole volume every step;
                                      enables SESNT_FIELD_ROT_* after any step (without it they
                                      are available after the steps of a rotation snapshot) */
+#define SESNT_FLAG_AUTOTUNE 512u  /* sesnt_set_model applies the tuning cache's choice for this GPU
+                                     and grid, or runs sesnt_tune and caches its choice */
+
+/* element-kernel variants (sesnt_set_element_variant); every variant computes
+ * the same step, up to the order of the atomic adds */
+#define SESNT_ELEMENT_AUTO 0        /* the launch rules: staged for SLS degrees 4-7, paired for even
+                                       elastic batches, else one point per thread */
+#define SESNT_ELEMENT_POINT 1       /* one thread per element-local point */
+#define SESNT_ELEMENT_PAIR 2        /* two simulations per thread (even elastic batches) */
+#define SESNT_ELEMENT_STAGE 3       /* SLS state staged by bulk copy, stored by bulk copy (degrees 4-7) */
+#define SESNT_ELEMENT_STAGE_REG 4   /* the same, stored from registers */
+#define SESNT_ELEMENT_PERSISTENT 5  /* persistent blocks fed by bulk copies */
+#define SESNT_ELEMENT_COLUMNS 6     /* one thread per (i, j) column of an element (elastic); arg
+                                       selects the resident blocks per SM the kernel is sized for
+                                       (0: 4, 1: 5, 2: 6, 3: 8) */
 
 /* source kinds (sesnt_add_source) */
 #define SESNT_SOURCE_MT 0 /* moment tensor: comp = Mxx Mxy Mxz Myy Myz Mzz */
@@ -226,6 +241,30 @@ int sesnt_run_profiled(sesnt_t *h, int it0, int nsteps, float ms[4]);
 
 /* Waits for all work queued on the handle. */
 int sesnt_synchronize(sesnt_t *h);
+
+/* No counterpart in the reference. Tunes the element kernel on this handle's
+ * grid, precision and batch: times every variant that computes this step
+ * (one point per thread, paired simulations, one thread per column at four
+ * register budgets, the staged kernel with bulk or register stores and
+ * 0/4/8/16 KB copy pieces, the persistent kernel) with CUDA events on the
+ * handle's stream, keeps the fastest and appends it to the tuning cache
+ * ($SESNT_TUNE_CACHE, else $HOME/.cache/sesnt-tune.txt), keyed by GPU name,
+ * SM count, degree, precision, SLS, anisotropy, batch and grid. Runs the
+ * kernel on the zero wavefield, which it leaves zero: call it after
+ * sesnt_set_model or sesnt_reset and before stepping (SESNT_ESTATE
+ * otherwise). report (may be NULL) receives the timings as text.
+ * Synchronous. */
+int sesnt_tune(sesnt_t *h, char *report, int report_len);
+
+/* No counterpart in the reference. Sets the element-kernel variant
+ * (SESNT_ELEMENT_*), its argument and the bulk-copy piece size in bytes
+ * (a multiple of 16, 0 = one copy per state unit; default 8192). A variant
+ * the handle's configuration does not have falls back to the launch rules. */
+int sesnt_set_element_variant(sesnt_t *h, int variant, int arg, int piece);
+
+/* The element kernel a step of this handle launches (its name) and the
+ * current choice[3] = {variant, arg, piece} (choice may be NULL). */
+int sesnt_element_kernel(const sesnt_t *h, char *name, int name_len, int choice[3]);
 
 /* Zeroes the wavefield, memory variables and seismograms (model kept) and
  * clears the error word of an earlier SESNT_ETIMEOUT. */

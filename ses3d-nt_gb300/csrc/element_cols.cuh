@@ -1,0 +1,229 @@
+// Elastic element kernel with one thread per (i, j) column of an element
+// (k_element_cols), for batched elastic steps. A block holds G (element,
+// simulation) units, consecutive in the element-major state order, and each
+// unit's P*P threads own its columns: a thread keeps its column's velocity
+// (3 x P values) and its z-direction fluxes (3 x P) in registers, so the
+// z line contractions of the strain (src/evolution.f90:136-144) and of the
+// weak divergence (:350-356) read no shared memory. Only the x and y
+// contractions go through per-unit slabs: per point and simulation that is
+// 3 velocity stores + 30 loads and 6 flux stores + 30 loads, against 12
+// stores + 90 loads with one thread per point (k_element, k_element_pair),
+// whose batched elastic launches were bound by the shared-memory data pipe
+// (L1 90% busy, 36 M wavefronts on the 12x12x8 grid with 64 simulations).
+// The derivative-table columns a thread contracts with (x and y, strain and
+// divergence) sit in registers; the z ones are uniform across the block and
+// are read as shared-memory broadcasts. Per point, the arithmetic and its
+// order are those of k_element (strain_contract, point_stress,
+// point_divergence).
+#pragma once
+
+namespace sesnt {
+
+template <int N>
+struct ColCfg {
+    static constexpr int P = N + 1, PP = P * P, NP = P * P * P;
+    // units per block: as many whole columns sets as fit 128 threads
+    static constexpr int G = PP <= 128 ? 128 / PP : 1;
+    static constexpr int NT = ((G * PP + 31) / 32) * 32;
+    static constexpr size_t SMEM_T = 4 * PP + (size_t)G * 9 * NP;  // values of T: tables, v + x/y fluxes
+};
+
+template <int N, typename T, bool ANISO, int MINB>
+__global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols(const StepArgs<T> a) {
+    using C = ColCfg<N>;
+    constexpr int P = C::P, PP = C::PP, NP = C::NP, G = C::G, NT = C::NT;
+    constexpr int NPS = state_stride(NP);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sD = reinterpret_cast<T *>(smem_raw);  // [4][P*P]: Dx Dy Dz (scaled) | Dt
+    const int t = threadIdx.x;
+    for (int x = t; x < 4 * PP; x += NT) sD[x] = a.tabD[x];
+    const int gl = t / PP;
+    const int c = t - gl * PP;
+    const int i = c % P, j = c / P;
+    T *sv = sD + 4 * PP + (size_t)gl * 9 * NP;  // this unit's [3][NP] velocity slab
+    T *sx = sv + 3 * NP;                        // [3][NP] x fluxes (xx, xy, xz weighted)
+    T *sy = sx + 3 * NP;                        // [3][NP] y fluxes
+    const long long units = (long long)a.nel * a.S;
+    const long long unit = (long long)blockIdx.x * G + gl;
+    const size_t nuni = (size_t)a.nuni, nloc = (size_t)a.nloc;
+    int e = 0, s = 0, ex = 0, ey = 0, ez = 0;
+    bool act = gl < G && unit < units;
+    if (act) {
+        e = (int)(unit / a.S);
+        s = (int)(unit - (long long)e * a.S);
+        ex = e % a.nx;
+        ey = (e / a.nx) % a.ny;
+        ez = e / (a.nx * a.ny);
+        act = in_range(unique_index<N>(a.NXU, a.NYU, ex, ey, ez, i, j, N), nuni, a.err) &&
+              in_range((size_t)e * NP + c + (size_t)PP * N, nloc, a.err) &&
+              in_range((size_t)unit * 6 * NPS + 5 * NPS + c + (size_t)PP * N, (size_t)units * 6 * NPS, a.err);
+    }
+    const size_t kstep = (size_t)a.NXU * a.NYU;  // unique-index stride of k
+    const size_t u0 = act ? unique_index<N>(a.NXU, a.NYU, ex, ey, ez, i, j, 0) : 0;
+    const size_t l0 = (size_t)e * NP + c;        // element-local index of (i, j, 0)
+    T *sig = a.sig + (size_t)unit * 6 * NPS + c;
+    T vc[3][P];  // this column's velocity
+    if (act) {
+        const T *vs = a.v + (size_t)s * 3 * nuni;
+#pragma unroll
+        for (int k = 0; k < P; ++k) {
+            const size_t u = u0 + k * kstep;
+            vc[0][k] = vs[u];
+            vc[1][k] = vs[nuni + u];
+            vc[2][k] = vs[2 * nuni + u];
+        }
+#pragma unroll
+        for (int k = 0; k < P; ++k) {
+            sv[c + PP * k] = vc[0][k];
+            sv[NP + c + PP * k] = vc[1][k];
+            sv[2 * NP + c + PP * k] = vc[2][k];
+        }
+    }
+    // material and stress of point k = 0, in flight across the barrier
+    T lam = 0, mu = 0, cA = 0, cB = 0, cC = 0, sg[6] = {0, 0, 0, 0, 0, 0};
+    auto load_point = [&](int k, T &l, T &m_, T &A, T &B, T &Cc, T (&sgk)[6]) {
+        const size_t li = l0 + (size_t)PP * k;
+        l = ld_stream(a.lam + li);
+        m_ = ld_stream(a.mu + li);
+        if constexpr (ANISO) {
+            A = ld_stream(a.A + li);
+            B = ld_stream(a.B + li);
+            Cc = ld_stream(a.C + li);
+        }
+#pragma unroll
+        for (int q = 0; q < 6; ++q) sgk[q] = ld_stream(sig + q * NPS + PP * k);
+    };
+    if (act) load_point(0, lam, mu, cA, cB, cC, sg);
+    __syncthreads();  // tables and velocity slabs
+    const T *Dx = sD, *Dy = sD + PP, *Dz = sD + 2 * PP, *Dt = sD + 3 * PP;
+    T dxi[P], dyj[P];
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+        dxi[q] = Dx[q * P + i];
+        dyj[q] = Dy[q * P + j];
+    }
+    T zf[3][P];  // z fluxes of this column: xz, yz, zz weighted (contracted along k)
+    const T m0[6][1] = {{0}, {0}, {0}, {0}, {0}, {0}};
+#pragma unroll
+    for (int k = 0; k < P; ++k) {
+        T nlam = 0, nmu = 0, nA = 0, nB = 0, nC = 0, nsg[6] = {0, 0, 0, 0, 0, 0};
+        if (k + 1 < P && act) load_point(k + 1, nlam, nmu, nA, nB, nC, nsg);
+        if (act) {
+            T ev[9];
+#pragma unroll
+            for (int x = 0; x < 9; ++x) ev[x] = 0;
+            const T *row = sv + P * (j + P * k);  // x line (q, j, k)
+            const T *col = sv + i + PP * k;       // y line (i, q, k)
+#pragma unroll
+            for (int q = 0; q < P; ++q) {
+                const T dx = dxi[q], dy = dyj[q], dz = Dz[q * P + k];
+                ev[0] += row[q] * dx;
+                ev[1] += row[NP + q] * dx;
+                ev[2] += row[2 * NP + q] * dx;
+                ev[3] += col[P * q] * dy;
+                ev[4] += col[NP + P * q] * dy;
+                ev[5] += col[2 * NP + P * q] * dy;
+                ev[6] += vc[0][q] * dz;
+                ev[7] += vc[1][q] * dz;
+                ev[8] += vc[2][q] * dz;
+            }
+            T sn[6], gw[3];
+            point_stress<N, T, 0, ANISO>(a, ev, vc[0][k], vc[1][k], vc[2][k], i, j, k, ex, ey, ez, lam, mu, T(0), cA,
+                                         cB, cC, sg, m0, sig + PP * k, nullptr, NPS, nloc, nullptr, sn, gw);
+            const int p = c + PP * k;
+            sx[p] = sn[0] * gw[0];
+            sx[NP + p] = sn[1] * gw[0];
+            sx[2 * NP + p] = sn[2] * gw[0];
+            sy[p] = sn[1] * gw[1];
+            sy[NP + p] = sn[3] * gw[1];
+            sy[2 * NP + p] = sn[4] * gw[1];
+            zf[0][k] = sn[2] * gw[2];
+            zf[1][k] = sn[4] * gw[2];
+            zf[2][k] = sn[5] * gw[2];
+        }
+        lam = nlam;
+        mu = nmu;
+        cA = nA;
+        cB = nB;
+        cC = nC;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) sg[q] = nsg[q];
+    }
+    __syncthreads();  // x and y flux slabs
+    if (!act) return;
+    T dti[P], dtj[P];
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+        dti[q] = Dt[i * P + q];
+        dtj[q] = Dt[j * P + q];
+    }
+    T *F = a.F + (size_t)s * 3 * nuni;
+#pragma unroll
+    for (int k = 0; k < P; ++k) {
+        T fx = 0, fy = 0, fz = 0;
+        const T *row = sx + P * (j + P * k);
+        const T *col = sy + i + PP * k;
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            const T di = dti[q], dj = dtj[q], dk = Dt[k * P + q];
+            fx += zf[0][q] * dk + col[P * q] * dj + row[q] * di;
+            fy += zf[1][q] * dk + col[NP + P * q] * dj + row[NP + q] * di;
+            fz += zf[2][q] * dk + col[2 * NP + P * q] * dj + row[2 * NP + q] * di;
+        }
+        const size_t u = u0 + k * kstep;
+        atomicAdd(F + u, fx);
+        atomicAdd(F + nuni + u, fy);
+        atomicAdd(F + 2 * nuni + u, fz);
+    }
+}
+
+// Resident blocks per SM the column kernel is sized for (FP32); FP64 uses 1
+// (as k_element). Selected per grid by the tuner among the instantiated
+// values.
+constexpr int kColsMinb[] = {4, 5, 6, 8};
+
+template <int N, typename T, bool ANISO, int MINB>
+int launch_element_cols_m(const StepArgs<T> &a, void *stream) {
+    using C = ColCfg<N>;
+    const long long units = (long long)a.nel * a.S;
+    const size_t smem = sizeof(T) * C::SMEM_T;
+    if (smem > kMaxSmemPerBlock) return 1;
+    k_element_cols<N, T, ANISO, MINB><<<(unsigned)((units + C::G - 1) / C::G), C::NT, smem, (cudaStream_t)stream>>>(a);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+// minb_idx selects kColsMinb[] (FP32); returns 1 if this configuration has
+// no column kernel (the caller falls back).
+template <int N, typename T, bool ANISO>
+int launch_element_cols(const StepArgs<T> &a, int minb_idx, void *stream) {
+    if constexpr (sizeof(T) == 8) {
+        return launch_element_cols_m<N, T, ANISO, 1>(a, stream);
+    } else {
+        switch (minb_idx) {
+            case 0: return launch_element_cols_m<N, T, ANISO, kColsMinb[0]>(a, stream);
+            case 1: return launch_element_cols_m<N, T, ANISO, kColsMinb[1]>(a, stream);
+            case 2: return launch_element_cols_m<N, T, ANISO, kColsMinb[2]>(a, stream);
+            default: return launch_element_cols_m<N, T, ANISO, kColsMinb[3]>(a, stream);
+        }
+    }
+}
+
+template <int N, typename T, bool ANISO, int MINB>
+int prepare_element_cols_m() {
+    const size_t smem = sizeof(T) * ColCfg<N>::SMEM_T;
+    if (smem <= 48 * 1024 || smem > kMaxSmemPerBlock) return 0;
+    return cudaFuncSetAttribute(k_element_cols<N, T, ANISO, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem) == cudaSuccess ? 0 : -1;
+}
+
+template <int N, typename T, bool ANISO>
+int prepare_element_cols() {
+    if constexpr (sizeof(T) == 8) return prepare_element_cols_m<N, T, ANISO, 1>();
+    else
+        return prepare_element_cols_m<N, T, ANISO, kColsMinb[0]>() || prepare_element_cols_m<N, T, ANISO, kColsMinb[1]>() ||
+                       prepare_element_cols_m<N, T, ANISO, kColsMinb[2]>() || prepare_element_cols_m<N, T, ANISO, kColsMinb[3]>()
+                   ? -1
+                   : 0;
+}
+
+}  // namespace sesnt

@@ -65,24 +65,18 @@ __device__ __forceinline__ bool tma_try_wait(uint32_t mbar, uint32_t parity, int
     return done != 0;
 }
 
-// Stages of the bulk-copy pipeline: loads run NSTAGE-1 elements ahead.
-// Bulk copies of one state unit are issued in pieces of at most this many
-// bytes (a multiple of 16; 0: one copy per unit). The 33 KB units of degree
-// 6 load 2.2% faster in 8 KB pieces than as one copy; degree 4 (12 KB) is the
-// same either way.
-#ifndef SESNT_BULK_PIECE
-#define SESNT_BULK_PIECE 8192
-#endif
+// Bulk copies of one state unit are issued in pieces of at most `piece`
+// bytes (StepArgs::piece, a multiple of 16; 0: one copy per unit), so every
+// piece starts 16-byte aligned inside the 16-byte aligned unit. The 33 KB
+// units of degree 6 load 2.2% faster in 8 KB pieces than as one copy; degree
+// 4 (12 KB) is the same either way. The tuner sweeps the size per grid.
 template <typename T>
-__device__ __forceinline__ void tma_load_unit(T *dst, const T *src, uint32_t bytes, uint32_t mbar) {
-    if constexpr (SESNT_BULK_PIECE > 0) {
-        for (uint32_t off = 0; off < bytes; off += SESNT_BULK_PIECE)
-            tma_load(tma_smem(reinterpret_cast<unsigned char *>(dst) + off),
-                     reinterpret_cast<const unsigned char *>(src) + off,
-                     bytes - off < (uint32_t)SESNT_BULK_PIECE ? bytes - off : (uint32_t)SESNT_BULK_PIECE, mbar);
-    } else {
-        tma_load(tma_smem(dst), src, bytes, mbar);
-    }
+__device__ __forceinline__ void tma_load_unit(T *dst, const T *src, uint32_t bytes, uint32_t mbar, int piece) {
+    const uint32_t pc = piece > 0 ? ((uint32_t)piece & ~15u) : bytes;
+    const uint32_t step = pc > 0 ? pc : bytes;
+    for (uint32_t off = 0; off < bytes; off += step)
+        tma_load(tma_smem(reinterpret_cast<unsigned char *>(dst) + off), reinterpret_cast<const unsigned char *>(src) + off,
+                 bytes - off < step ? bytes - off : step, mbar);
 }
 
 #ifndef SESNT_TMA_STAGES
@@ -142,7 +136,7 @@ __global__ void __launch_bounds__(TmaCfg<N, T, NSLS>::NT, TmaCfg<N, T, NSLS>::MI
         unsigned char *st = stage0 + (size_t)b * C::STAGE_BYTES;
         const uint32_t mb = tma_smem(mbar + b);
         tma_expect(mb, C::STAGE_BYTES);
-        tma_load_unit(reinterpret_cast<T *>(st), a.sig + (size_t)g * C::UNIT, C::STAGE_BYTES, mb);
+        tma_load_unit(reinterpret_cast<T *>(st), a.sig + (size_t)g * C::UNIT, C::STAGE_BYTES, mb, a.piece);
     };
     if (t == 0)
         for (int k = 0; k < NSTAGE - 1 && k < count; ++k) issue_load(k);
@@ -253,8 +247,8 @@ __global__ void __launch_bounds__(TmaCfg<N, T, NSLS>::NT, TmaCfg<N, T, NSLS>::MI
 // before the velocity gather, so it travels during the gather, the staging
 // barrier and the line contractions, and the state costs no per-thread load
 // instructions or registers. The updated state goes back
-// into the stage and out by bulk store (STORE), or for degree 6 from
-// registers as in k_element. Measured on 3-SLS FP32 grids of 6-7 M points
+// into the stage and out by bulk store (STORE), or from registers as in
+// k_element (the default for degree 6). Measured on 3-SLS FP32 grids of 6-7 M points
 // against k_element: 3.2/4.1/10.1/10.8% faster for degrees 4/5/6/7 (degree
 // 6: 9.4% with the bulk store); FP64 unchanged. On elastic grids (one 3 KB
 // chunk per element) it was 1-3% slower for degrees 4-6, so they keep
@@ -267,14 +261,14 @@ struct StageCfg {
     static constexpr uint32_t STAGE_BYTES = (uint32_t)(UNIT * sizeof(T));  // one unit, a multiple of 16
     static constexpr size_t SMALL = sizeof(T) * (4 * P * P + 12 * NP);
     static constexpr size_t SMEM = STAGE_BYTES + ((SMALL + 15) / 16) * 16 + 8;
-    static constexpr bool STORE = N != 6;
+    static constexpr bool STORE_DEFAULT = N != 6;
 #ifndef SESNT_MINB_STAGE
 #define SESNT_MINB_STAGE 8
 #endif
     static constexpr int MINB = sizeof(T) == 4 ? (NT <= 128 ? SESNT_MINB_STAGE : ElemCfg<N>::MINB) : 1;
 };
 
-template <int N, typename T, int NSLS, bool ANISO>
+template <int N, typename T, int NSLS, bool ANISO, bool STORE>
 __global__ void __launch_bounds__(StageCfg<N, T, NSLS>::NT, StageCfg<N, T, NSLS>::MINB) k_element_stage(const StepArgs<T> a) {
     using C = StageCfg<N, T, NSLS>;
     constexpr int P = C::P, NP = C::NP, NPS = C::NPS, NT = C::NT, MS = NSLS > 0 ? NSLS : 1;
@@ -299,7 +293,7 @@ __global__ void __launch_bounds__(StageCfg<N, T, NSLS>::NT, StageCfg<N, T, NSLS>
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         if (!a.drop_completion) {  // failure-detection test: the stage never lands
             tma_expect(mb, C::STAGE_BYTES);
-            tma_load_unit(st, a.sig + sb * C::UNIT, C::STAGE_BYTES, mb);
+            tma_load_unit(st, a.sig + sb * C::UNIT, C::STAGE_BYTES, mb, a.piece);
             issued = true;
         }
     }
@@ -344,7 +338,7 @@ __global__ void __launch_bounds__(StageCfg<N, T, NSLS>::NT, StageCfg<N, T, NSLS>
 #pragma unroll
                 for (int q = 0; q < NSLS; ++q) m[c][q] = st[6 * NPS + (c * NSLS + q) * NPS + p];
         }
-        if constexpr (C::STORE)
+        if constexpr (STORE)
             point_update<N, T, NSLS, ANISO, false, true>(a, ev, vx, vy, vz, p, i, j, k, ex, ey, ez, lam, mu, tau, cA,
                                                          cB, cC, sg, m, st + p, st + 6 * NPS + p, NPS, nloc, sf,
                                                          nullptr);
@@ -354,9 +348,9 @@ __global__ void __launch_bounds__(StageCfg<N, T, NSLS>::NT, StageCfg<N, T, NSLS>
                                             nullptr);
     }
     // updated state in the stage: visible to the bulk-copy engine after the barrier
-    if constexpr (C::STORE) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    if constexpr (STORE) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     const bool ok = __syncthreads_and(landed) != 0;
-    if (C::STORE && ok && t == 0) {
+    if (STORE && ok && t == 0) {
         tma_store(a.sig + sb * C::UNIT, tma_smem(st), C::STAGE_BYTES);
         tma_commit();
     }
@@ -374,7 +368,7 @@ __global__ void __launch_bounds__(StageCfg<N, T, NSLS>::NT, StageCfg<N, T, NSLS>
         // the block's shared memory is released
         if (issued) tma_try_wait(tma_smem(mbar), 0, a.wait_polls);
     }
-    if (C::STORE && ok && t == 0) tma_wait_read<0>();  // the stores have read the stage before it is released
+    if (STORE && ok && t == 0) tma_wait_read<0>();  // the stores have read the stage before it is released
 }
 
 template <int N, typename T, int NSLS, bool ANISO>
@@ -382,16 +376,22 @@ int prepare_element_stage() {
     using C = StageCfg<N, T, NSLS>;
     if (C::SMEM <= 48 * 1024) return 0;
     if (C::SMEM > kMaxSmemPerBlock) return 0;
-    return cudaFuncSetAttribute(k_element_stage<N, T, NSLS, ANISO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)C::SMEM) == cudaSuccess ? 0 : -1;
+    for (auto *f : {k_element_stage<N, T, NSLS, ANISO, true>, k_element_stage<N, T, NSLS, ANISO, false>})
+        if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM) != cudaSuccess)
+            return -1;
+    return 0;
 }
 
+// store: 1 bulk store, 0 register stores, -1 the degree's default.
 template <int N, typename T, int NSLS, bool ANISO>
-int launch_element_stage(const StepArgs<T> &a, void *stream) {
+int launch_element_stage(const StepArgs<T> &a, int store, void *stream) {
     using C = StageCfg<N, T, NSLS>;
     if (C::SMEM > kMaxSmemPerBlock) return 1;
     const long long blocks = (long long)a.nel * a.S;
-    k_element_stage<N, T, NSLS, ANISO><<<(unsigned)blocks, C::NT, C::SMEM, (cudaStream_t)stream>>>(a);
+    if (store < 0 ? C::STORE_DEFAULT : store != 0)
+        k_element_stage<N, T, NSLS, ANISO, true><<<(unsigned)blocks, C::NT, C::SMEM, (cudaStream_t)stream>>>(a);
+    else
+        k_element_stage<N, T, NSLS, ANISO, false><<<(unsigned)blocks, C::NT, C::SMEM, (cudaStream_t)stream>>>(a);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 

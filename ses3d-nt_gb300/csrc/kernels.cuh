@@ -244,16 +244,20 @@ __device__ __forceinline__ void stress_rates(T exx, T eyy, T ezz, T exy, T exz, 
 }
 
 // The rest of one element-local point's step, from its raw velocity gradient
-// e[9] (layout of strain_contract) and velocity. DU: integrate this point's
-// displacement gradient `du` (stride nloc); a compile-time switch, since even
-// a skipped branch measured 1.5% on the step. SMEM: sig/mem point into shared
-// memory (plain stores instead of streaming global stores).
+// e[9] (layout of strain_contract) and velocity, up to the stored stress:
+// completion, stress rate, integration, the tapered stress and memory
+// variables stored, and in sn[6] (xx xy xz yy yz zz) the integrated stress
+// before the taper with gw[3] its metric weights for the weak divergence.
+// DU: integrate this point's displacement gradient `du` (stride nloc); a
+// compile-time switch, since even a skipped branch measured 1.5% on the
+// step. SMEM: sig/mem point into shared memory (plain stores instead of
+// streaming global stores).
 template <int N, typename T, int NSLS, bool ANISO, bool DU = false, bool SMEM = false>
-__device__ __forceinline__ void point_update(const StepArgs<T> &a, const T (&e)[9], T vx, T vy, T vz, int p, int i,
-                                             int j, int k, int ex, int ey, int ez, T lam, T mu, T tau, T cA, T cB,
-                                             T cC, const T (&sg)[6], const T (&m)[6][NSLS > 0 ? NSLS : 1], T *sig,
-                                             T *mem, size_t cs, size_t nloc, T *my, T *du) {
-    constexpr int P = N + 1, NP = P * P * P;
+__device__ __forceinline__ void point_stress(const StepArgs<T> &a, const T (&e)[9], T vx, T vy, T vz, int i, int j,
+                                             int k, int ex, int ey, int ez, T lam, T mu, T tau, T cA, T cB, T cC,
+                                             const T (&sg)[6], const T (&m)[6][NSLS > 0 ? NSLS : 1], T *sig, T *mem,
+                                             size_t cs, size_t nloc, T *du, T (&sn)[6], T (&gw)[3]) {
+    constexpr int P = N + 1;
     T g[9];
     complete_gradient<N, T>(a, e, vx, vy, vz, i, k, ex, ez, g);
     T exx = g[kDuXX], eyy = g[kDuYY], ezz = g[kDuZZ], exy = g[kDuXY], eyx = g[kDuYX], exz = g[kDuXZ],
@@ -310,20 +314,35 @@ __device__ __forceinline__ void point_update(const StepArgs<T> &a, const T (&e)[
             }
         }
     }
-    // metric-weighted stresses for the weak divergence
+    // metric weights of the stresses in the weak divergence
     const T W = a.w[i] * a.w[j] * a.w[k];
-    const T gx = W * rs * a.c1;
-    const T gy = W * rr * a.c2;
-    const T gz = W * (rr * rs) * a.c3;
-    my[0 * NP + p] = sxx * gx;
-    my[1 * NP + p] = sxy * gy;
-    my[2 * NP + p] = sxz * gz;
-    my[3 * NP + p] = sxy * gx;
-    my[4 * NP + p] = syy * gy;
-    my[5 * NP + p] = syz * gz;
-    my[6 * NP + p] = sxz * gx;
-    my[7 * NP + p] = syz * gy;
-    my[8 * NP + p] = szz * gz;
+    gw[0] = W * rs * a.c1;
+    gw[1] = W * rr * a.c2;
+    gw[2] = W * (rr * rs) * a.c3;
+    sn[0] = sxx; sn[1] = sxy; sn[2] = sxz; sn[3] = syy; sn[4] = syz; sn[5] = szz;
+}
+
+// point_stress, then the metric-weighted stresses for the weak divergence
+// written to the flux slab `my` (9 x NP): entries 0, 3, 6 are contracted
+// along x, 1, 4, 7 along y, 2, 5, 8 along z (point_divergence).
+template <int N, typename T, int NSLS, bool ANISO, bool DU = false, bool SMEM = false>
+__device__ __forceinline__ void point_update(const StepArgs<T> &a, const T (&e)[9], T vx, T vy, T vz, int p, int i,
+                                             int j, int k, int ex, int ey, int ez, T lam, T mu, T tau, T cA, T cB,
+                                             T cC, const T (&sg)[6], const T (&m)[6][NSLS > 0 ? NSLS : 1], T *sig,
+                                             T *mem, size_t cs, size_t nloc, T *my, T *du) {
+    constexpr int P = N + 1, NP = P * P * P;
+    T sn[6], gw[3];
+    point_stress<N, T, NSLS, ANISO, DU, SMEM>(a, e, vx, vy, vz, i, j, k, ex, ey, ez, lam, mu, tau, cA, cB, cC, sg, m,
+                                              sig, mem, cs, nloc, du, sn, gw);
+    my[0 * NP + p] = sn[0] * gw[0];
+    my[1 * NP + p] = sn[1] * gw[1];
+    my[2 * NP + p] = sn[2] * gw[2];
+    my[3 * NP + p] = sn[1] * gw[0];
+    my[4 * NP + p] = sn[3] * gw[1];
+    my[5 * NP + p] = sn[4] * gw[2];
+    my[6 * NP + p] = sn[2] * gw[0];
+    my[7 * NP + p] = sn[4] * gw[1];
+    my[8 * NP + p] = sn[5] * gw[2];
 }
 
 // One element-local point of the step with CUDA-core contractions.
@@ -930,6 +949,7 @@ int prepare_variant() {
 
 }  // namespace sesnt
 
+#include "element_cols.cuh"
 #include "element_tc.cuh"
 #include "element_tma.cuh"
 
@@ -949,6 +969,7 @@ int prepare_element() {
         return -1;
     if constexpr (ElemCfg<N>::EPB == 1)
         if (prepare_element_stage<N, T, kNsls, false>() || prepare_element_stage<N, T, kNsls, true>()) return -1;
+    if (prepare_element_cols<N, T, false>() || prepare_element_cols<N, T, true>()) return -1;
     return 0;
 }
 
@@ -961,22 +982,109 @@ int launch_element_bulk(const StepArgs<T> &a, bool sls, bool aniso, void *stream
     return aniso ? launch_element_tma<N, T, 0, true>(a, stream) : launch_element_tma<N, T, 0, false>(a, stream);
 }
 
+// The element kernel one step launches, decided on the host from the
+// handle's configuration (plan_element) so that the launcher, the tuner and
+// the kernel name a caller reads agree.
+enum class ElemKernel : int { Tc, Point, Pair, StageBulk, StageReg, Persistent, Columns };
+
+inline const char *elem_kernel_name(ElemKernel k) {
+    switch (k) {
+        case ElemKernel::Tc: return "k_element_tc";
+        case ElemKernel::Point: return "k_element";
+        case ElemKernel::Pair: return "k_element_pair";
+        case ElemKernel::StageBulk: return "k_element_stage";
+        case ElemKernel::StageReg: return "k_element_stage (register stores)";
+        case ElemKernel::Persistent: return "k_element_tma";
+        case ElemKernel::Columns: return "k_element_cols";
+    }
+    return "?";
+}
+
+template <int N, typename T>
+bool has_persistent(bool sls, bool aniso) {
+    using C0 = TmaCfg<N, T, 0>;
+    using C3 = TmaCfg<N, T, kNsls>;
+    if (sls) {
+        if (C3::SMEM > kMaxSmemPerBlock) return false;
+        return (aniso ? TmaLaunch<N, T, kNsls, true>::blocks : TmaLaunch<N, T, kNsls, false>::blocks) > 0;
+    }
+    if (C0::SMEM > kMaxSmemPerBlock) return false;
+    return (aniso ? TmaLaunch<N, T, 0, true>::blocks : TmaLaunch<N, T, 0, false>::blocks) > 0;
+}
+
+template <int N, typename T>
+constexpr bool has_staged() {
+    return ElemCfg<N>::EPB == 1 && StageCfg<N, T, kNsls>::SMEM <= kMaxSmemPerBlock;
+}
+
+template <int N, typename T>
+constexpr bool has_columns() {
+    return sizeof(T) * ColCfg<N>::SMEM_T <= kMaxSmemPerBlock;
+}
+
+// A variant chosen by the tuner or the caller (StepArgs::variant) where the
+// configuration has it; otherwise the rules: tensor-core contractions when
+// asked for; the persistent kernel when asked for; the staged kernel for SLS
+// steps of degrees 4-7; one point per thread, with paired simulations for
+// even elastic batches. The displacement gradient (du) is kept only by
+// k_element.
+template <int N, typename T>
+ElemKernel plan_element(const StepArgs<T> &a, bool sls, bool aniso) {
+    if (std::is_same_v<T, float> && a.contraction) return ElemKernel::Tc;
+    const bool even = a.S >= 2 && a.S % 2 == 0;
+    if (a.du) return ElemKernel::Point;
+    switch (a.variant) {
+        case kVarPoint: return ElemKernel::Point;
+        case kVarPair: if (!sls && even) return ElemKernel::Pair; break;
+        case kVarStage: if (sls && has_staged<N, T>()) return ElemKernel::StageBulk; break;
+        case kVarStageReg: if (sls && has_staged<N, T>()) return ElemKernel::StageReg; break;
+        case kVarPersistent: if (has_persistent<N, T>(sls, aniso)) return ElemKernel::Persistent; break;
+        case kVarColumns: if (!sls && has_columns<N, T>()) return ElemKernel::Columns; break;
+        default: break;
+    }
+    if (a.persistent && has_persistent<N, T>(sls, aniso)) return ElemKernel::Persistent;
+    if (sls && a.stage && has_staged<N, T>())
+        return StageCfg<N, T, kNsls>::STORE_DEFAULT ? ElemKernel::StageBulk : ElemKernel::StageReg;
+    if (!sls && even && a.pair) return ElemKernel::Pair;
+    return ElemKernel::Point;
+}
+
+template <int N, typename T>
+const char *element_name(const StepArgs<T> &a, bool sls, bool aniso) {
+    return elem_kernel_name(plan_element<N, T>(a, sls, aniso));
+}
+
 template <int N, typename T>
 int launch_element(const StepArgs<T> &a, bool sls, bool aniso, void *stream) {
-    if constexpr (std::is_same_v<T, float>)
-        if (a.contraction) return launch_element_tc<N>(a, sls, aniso, stream);
-    if (a.persistent && !a.du) {
-        const int r = launch_element_bulk<N, T>(a, sls, aniso, stream);
-        if (r <= 0) return r;
-    }
-    if constexpr (ElemCfg<N>::EPB == 1)
-        if (sls && a.stage && !a.du) {
-            const int r = aniso ? launch_element_stage<N, T, kNsls, true>(a, stream)
-                                : launch_element_stage<N, T, kNsls, false>(a, stream);
-            if (r <= 0) return r;
+    const ElemKernel k = plan_element<N, T>(a, sls, aniso);
+    StepArgs<T> b = a;
+    switch (k) {
+        case ElemKernel::Tc:
+            if constexpr (std::is_same_v<T, float>) return launch_element_tc<N>(a, sls, aniso, stream);
+            return -1;
+        case ElemKernel::Persistent: {
+            const int r = launch_element_bulk<N, T>(a, sls, aniso, stream);
+            return r > 0 ? -1 : r;
         }
-    if (sls) return aniso ? launch_element_v<N, T, kNsls, true>(a, stream) : launch_element_v<N, T, kNsls, false>(a, stream);
-    return aniso ? launch_element_v<N, T, 0, true>(a, stream) : launch_element_v<N, T, 0, false>(a, stream);
+        case ElemKernel::StageBulk:
+        case ElemKernel::StageReg:
+            if constexpr (ElemCfg<N>::EPB == 1) {
+                const int store = k == ElemKernel::StageBulk ? 1 : 0;
+                const int r = aniso ? launch_element_stage<N, T, kNsls, true>(a, store, stream)
+                                    : launch_element_stage<N, T, kNsls, false>(a, store, stream);
+                return r > 0 ? -1 : r;
+            }
+            return -1;
+        case ElemKernel::Columns: {
+            const int r = aniso ? launch_element_cols<N, T, true>(a, a.variant_arg, stream)
+                                : launch_element_cols<N, T, false>(a, a.variant_arg, stream);
+            return r > 0 ? -1 : r;
+        }
+        case ElemKernel::Pair: b.pair = 1; break;
+        case ElemKernel::Point: b.pair = 0; break;
+    }
+    if (sls) return aniso ? launch_element_v<N, T, kNsls, true>(b, stream) : launch_element_v<N, T, kNsls, false>(b, stream);
+    return aniso ? launch_element_v<N, T, 0, true>(b, stream) : launch_element_v<N, T, 0, false>(b, stream);
 }
 
 template <int N, typename T>
@@ -1039,7 +1147,7 @@ const LpdOps<T> *lpd_ops_n() {
         &launch_element<N, T>,        &launch_node<N, T>,        &launch_sources<N, T>,
         &launch_receivers<N, T>,      &launch_inv_mass<N, T>,    &launch_gather_local<N, T>,
         &launch_scatter_unique<N, T>, &launch_taper_local<N, T>, &launch_rot_strain<N, T>,
-        &launch_derived<N, T>,        &prepare_element<N, T>,    ElemCfg<N>::NT,
+        &launch_derived<N, T>,        &prepare_element<N, T>,    &element_name<N, T>,       ElemCfg<N>::NT,
         sizeof(T) * (4 * ElemCfg<N>::P * ElemCfg<N>::P + ElemCfg<N>::EPB * 12 * ElemCfg<N>::NP)};
     return &ops;
 }

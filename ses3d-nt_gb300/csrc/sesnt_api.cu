@@ -9,8 +9,11 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <limits>
+#include <sstream>
 #include <memory>
 #include <string>
 #include <vector>
@@ -354,6 +357,11 @@ struct sesnt_handle {
     cudaGraphExec_t ladder[kLadder] = {};
     // v_ptp: device reduction words and the mapped host words of the result
     unsigned long long *d_ptp = nullptr, *h_ptp = nullptr, *h_ptp_dev = nullptr;
+    // element-kernel variant (ElementVariant), its argument and the bulk-copy
+    // piece size: the launch rules by default, set by sesnt_tune (or the
+    // tuning cache under SESNT_FLAG_AUTOTUNE) or sesnt_set_element_variant
+    int variant = kVarAuto, variant_arg = 0, piece = 8192;
+    std::string tune_report;
     // kinetic energy: per-block partial sums (kinetic_blocks doubles)
     double *d_kin = nullptr;
     int sms = 0;  // multiprocessors of the handle's device (grid sizes of the reductions)
@@ -492,6 +500,9 @@ struct sesnt_handle {
         a.pair = (g.flags & SESNT_FLAG_NO_PAIR) ? 0 : 1;
         a.stage = (g.flags & SESNT_FLAG_NO_STAGE) ? 0 : 1;
         a.contraction = (g.flags & SESNT_FLAG_TC_TF32X3) ? 1 : ((g.flags & SESNT_FLAG_TC_BF16X3) ? 2 : 0);
+        a.variant = variant;
+        a.variant_arg = variant_arg;
+        a.piece = piece;
         a.two_over_d[0] = (T)two_over_d[0];
         a.two_over_d[1] = (T)two_over_d[1];
         a.two_over_d[2] = (T)two_over_d[2];
@@ -961,6 +972,20 @@ int build_graph(sesnt_t *h) {
     return SESNT_OK;
 }
 
+// Every graph a run of this handle can replay (runs of kGraphSteps, the
+// 16/8/4/2-step ladder and the single step), captured after a run's own
+// launches, so that the host captures while the device executes them and
+// later runs, of any length, replay without capturing.
+template <typename T>
+int prebuild_graphs(sesnt_t *h) {
+    int rc;
+    if (!h->graph && (rc = build_graph<T>(h))) return rc;
+    for (int q = 0; q < sesnt_handle::kLadder; ++q)
+        if (!h->ladder[q] && (rc = capture_steps<T>(h, 2 << q, &h->ladder[q], true))) return rc;
+    if (!h->graph1 && (rc = capture_steps<T>(h, 1, &h->graph1, false))) return rc;
+    return SESNT_OK;
+}
+
 // Steps it0 .. it0+nsteps-1 (prepared): graph replays (runs of kGraphSteps,
 // then the remainder as graphs of 16, 8, 4, 2 and 1 steps, so a short run
 // costs at most five graph launches), or direct launches without graphs.
@@ -1003,6 +1028,7 @@ int run_steps(sesnt_t *h, int it0, int nsteps) {
         if ((rc = enqueue_steps<T>(h, left))) return rc;
         h->mark(it0 + nsteps - 1);
     }
+    if (h->use_graph && (rc = prebuild_graphs<T>(h))) return rc;
     h->last_it = it0 + nsteps - 1;
     if (h->g.flags & SESNT_FLAG_ROTATION) h->rot_full_it = h->last_it;
     return SESNT_OK;
@@ -1175,6 +1201,8 @@ int get_field_impl(sesnt_t *h, int sim, int which, void *out, int out_prec) {
     return SESNT_OK;
 }
 
+int autotune(sesnt_t *h);
+
 template <typename T>
 int set_model_impl(sesnt_t *h, const float *rhoinv, const float *lambda, const float *mu, const float *a,
                    const float *b, const float *c, const float *q) {
@@ -1281,7 +1309,8 @@ int set_model_impl(sesnt_t *h, const float *rhoinv, const float *lambda, const f
     h->model_set = true;
     if ((rc = zero_state(h))) return rc;
     e = cudaStreamSynchronize(h->stream);
-    return e == cudaSuccess ? SESNT_OK : h->cuda_fail(e, "zeroing state");
+    if (e != cudaSuccess) return h->cuda_fail(e, "zeroing state");
+    return (h->g.flags & SESNT_FLAG_AUTOTUNE) ? autotune(h) : SESNT_OK;
 }
 
 template <typename T>
@@ -1397,6 +1426,183 @@ int assemble_impl(sesnt_t *h, float *field) {
     if (e != cudaSuccess) return h->cuda_fail(e, "assemble_field");
     export_layout(host.data(), field, h->nel, h->NP);
     return SESNT_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Tuner: element-kernel variant, tile shape and bulk-copy piece size per grid.
+// ---------------------------------------------------------------------------
+struct TuneChoice {
+    int variant, arg, piece;
+};
+
+// Candidates for this handle: every element kernel that computes this step
+// (tensor-core contractions change the arithmetic and are never chosen):
+// one point per thread; paired simulations (even elastic batches); one
+// thread per column at each instantiated resident-block count (elastic);
+// the staged kernel with bulk or register stores and four piece sizes (SLS);
+// the persistent kernel.
+std::vector<TuneChoice> tune_candidates(const sesnt_t *h) {
+    std::vector<TuneChoice> c = {{kVarPoint, 0, 8192}};
+    if (!h->sls) {
+        if (h->S % 2 == 0) c.push_back({kVarPair, 0, 8192});
+        for (int m = 0; m < 4; ++m) c.push_back({kVarColumns, m, 8192});
+    } else {
+        for (int v : {kVarStage, kVarStageReg})
+            for (int piece : {0, 4096, 8192, 16384}) c.push_back({v, 0, piece});
+    }
+    for (int piece : {0, 8192}) c.push_back({kVarPersistent, 0, piece});
+    return c;
+}
+
+std::string tune_key(const sesnt_t *h) {
+    cudaDeviceProp prop{};
+    if (cudaGetDeviceProperties(&prop, h->device) != cudaSuccess) {
+        cudaGetLastError();
+        std::snprintf(prop.name, sizeof prop.name, "unknown");
+    }
+    std::string name = prop.name;
+    for (char &ch : name)
+        if (ch == ' ' || ch == '|') ch = '_';
+    char buf[384];
+    std::snprintf(buf, sizeof buf, "%s|sm=%d|lpd=%d|prec=%d|sls=%d|aniso=%d|batch=%d|grid=%dx%dx%d|strain=%d", name.c_str(),
+                  h->sms, h->g.lpd, h->g.precision, h->sls ? kNsls : 0, h->aniso ? 1 : 0, h->S, h->g.nx, h->g.ny,
+                  h->g.nz, (h->g.flags & SESNT_FLAG_STRAIN) ? 1 : 0);
+    return buf;
+}
+
+std::string tune_cache_path() {
+    const char *p = std::getenv("SESNT_TUNE_CACHE");
+    if (p && *p) return p;
+    const char *home = std::getenv("HOME");
+    if (!home || !*home) return "";
+    return std::string(home) + "/.cache/sesnt-tune.txt";
+}
+
+// The last entry for `key` in the cache file: "key variant arg piece ms".
+bool tune_cache_lookup(const std::string &key, TuneChoice *out) {
+    const std::string path = tune_cache_path();
+    if (path.empty()) return false;
+    std::ifstream f(path);
+    std::string line;
+    bool found = false;
+    while (std::getline(f, line)) {
+        std::istringstream is(line);
+        std::string k;
+        TuneChoice c{};
+        if (is >> k >> c.variant >> c.arg >> c.piece && k == key && c.variant > kVarAuto && c.variant < kVarCount) {
+            *out = c;
+            found = true;
+        }
+    }
+    return found;
+}
+
+void tune_cache_store(const std::string &key, const TuneChoice &c, double ms) {
+    const std::string path = tune_cache_path();
+    if (path.empty()) return;
+    std::ofstream f(path, std::ios::app);
+    if (f) f << key << ' ' << c.variant << ' ' << c.arg << ' ' << c.piece << ' ' << ms << '\n';
+}
+
+// Times every candidate on the handle's own grid: the element kernel alone,
+// launched on the zero wavefield (which it leaves exactly zero: zero
+// velocity, stress and memory variables give zero rates and zero forces),
+// with CUDA events on the handle's stream, a few launches warm and then
+// enough launches for at least about 2 ms, best of 3 repeats. The fastest
+// becomes the handle's choice; the wavefield is zeroed again afterwards.
+template <typename T>
+int tune_impl(sesnt_t *h, TuneChoice *best_out, double *best_ms) {
+    const LpdOps<T> *o = ops<T>(h);
+    std::ostringstream rep;
+    rep << "tuning " << tune_key(h) << "\n";
+    TuneChoice best{kVarAuto, h->variant_arg, h->piece};
+    double best_t = 1e30;
+    std::vector<std::string> seen;
+    for (const TuneChoice &c : tune_candidates(h)) {
+        h->variant = c.variant;
+        h->variant_arg = c.arg;
+        h->piece = c.piece;
+        StepArgs<T> a = h->args<T>();
+        a.nsrc = 0;
+        const std::string name = o->element_name(a, h->sls, h->aniso);
+        // a variant the configuration does not have falls back to the rules: skip it
+        const bool applicable = (c.variant == kVarPoint && name == "k_element") ||
+                                (c.variant == kVarPair && name == "k_element_pair") ||
+                                (c.variant == kVarStage && name == "k_element_stage") ||
+                                (c.variant == kVarStageReg && name == "k_element_stage (register stores)") ||
+                                (c.variant == kVarPersistent && name == "k_element_tma") ||
+                                (c.variant == kVarColumns && name == "k_element_cols");
+        if (!applicable) continue;
+        auto launch = [&](int n) {
+            for (int q = 0; q < n; ++q)
+                if (o->element(a, h->sls, h->aniso, h->stream)) return false;
+            return true;
+        };
+        if (!launch(2)) return h->fail(SESNT_ECUDA, "tuning launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+        float ms1 = 0.0f;
+        cudaEventRecord(h->ev0, h->stream);
+        launch(1);
+        cudaEventRecord(h->ev1, h->stream);
+        cudaError_t e = cudaEventSynchronize(h->ev1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms1, h->ev0, h->ev1);
+        if (e != cudaSuccess) return h->cuda_fail(e, "tuning");
+        const int n = std::max(3, std::min(200, (int)(2.0 / std::max(ms1, 1e-3f))));
+        double t = 1e30;
+        for (int rep_i = 0; rep_i < 3; ++rep_i) {
+            float ms = 0.0f;
+            cudaEventRecord(h->ev0, h->stream);
+            if (!launch(n)) return h->fail(SESNT_ECUDA, "tuning launch failed");
+            cudaEventRecord(h->ev1, h->stream);
+            e = cudaEventSynchronize(h->ev1);
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+            if (e != cudaSuccess) return h->cuda_fail(e, "tuning");
+            t = std::min(t, (double)ms / n);
+        }
+        char line[256];
+        std::snprintf(line, sizeof line, "  %-34s variant %d arg %d piece %5d: %.4f ms\n", name.c_str(), c.variant,
+                      c.arg, c.piece, t);
+        rep << line;
+        if (t < best_t) {
+            best_t = t;
+            best = c;
+        }
+    }
+    int rc = h->wait_status();
+    if (rc) return rc;
+    h->variant = best.variant;
+    h->variant_arg = best.arg;
+    h->piece = best.piece;
+    char line[160];
+    std::snprintf(line, sizeof line, "chosen: variant %d arg %d piece %d (%.4f ms per element launch)\n", best.variant,
+                  best.arg, best.piece, best_t);
+    rep << line;
+    h->tune_report = rep.str();
+    *best_out = best;
+    *best_ms = best_t;
+    if ((rc = zero_state(h))) return rc;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    return e == cudaSuccess ? SESNT_OK : h->cuda_fail(e, "tuning");
+}
+
+// Under SESNT_FLAG_AUTOTUNE, after the model is set: the cached choice for
+// this GPU and grid, or a tuning run whose result is cached.
+int autotune(sesnt_t *h) {
+    if (h->g.flags & (SESNT_FLAG_TC_TF32X3 | SESNT_FLAG_TC_BF16X3)) return SESNT_OK;
+    const std::string key = tune_key(h);
+    TuneChoice c{};
+    if (tune_cache_lookup(key, &c)) {
+        h->variant = c.variant;
+        h->variant_arg = c.arg;
+        h->piece = c.piece;
+        h->drop_graph();
+        h->tune_report = "cached: " + key + "\n";
+        return SESNT_OK;
+    }
+    double ms = 0;
+    h->drop_graph();
+    const int rc = h->dbl ? tune_impl<double>(h, &c, &ms) : tune_impl<float>(h, &c, &ms);
+    if (rc == SESNT_OK) tune_cache_store(key, c, ms);
+    return rc;
 }
 
 size_t footprint(const sesnt_grid_t *g, bool aniso) {
@@ -1848,6 +2054,50 @@ int sesnt_kinetic_energy(sesnt_t *h, int sim, double *out) {
 int sesnt_assemble_field(sesnt_t *h, float *field) {
     if (!h || !field) return SESNT_EINVAL;
     return h->dbl ? assemble_impl<double>(h, field) : assemble_impl<float>(h, field);
+}
+
+int sesnt_tune(sesnt_t *h, char *report, int report_len) {
+    Range r("sesnt_tune");
+    if (!h) return SESNT_EINVAL;
+    if (!h->model_set) return h->fail(SESNT_ESTATE, "sesnt_set_model must be called before sesnt_tune");
+    if (h->last_it != 0)
+        return h->fail(SESNT_ESTATE, "sesnt_tune times the step on the zero wavefield: call it after sesnt_set_model "
+                                     "or sesnt_reset, before stepping");
+    if (h->g.flags & (SESNT_FLAG_TC_TF32X3 | SESNT_FLAG_TC_BF16X3))
+        return h->fail(SESNT_EUNSUPPORTED, "the tensor-core contractions have no variants to tune");
+    TuneChoice c{};
+    double ms = 0;
+    h->drop_graph();
+    const int rc = h->dbl ? tune_impl<double>(h, &c, &ms) : tune_impl<float>(h, &c, &ms);
+    if (rc) return rc;
+    tune_cache_store(tune_key(h), c, ms);
+    if (report && report_len > 0) std::snprintf(report, (size_t)report_len, "%s", h->tune_report.c_str());
+    return SESNT_OK;
+}
+
+int sesnt_set_element_variant(sesnt_t *h, int variant, int arg, int piece) {
+    if (!h) return SESNT_EINVAL;
+    if (variant < kVarAuto || variant >= kVarCount) return h->fail(SESNT_EINVAL, "unknown element variant %d", variant);
+    if (arg < 0 || arg > 3) return h->fail(SESNT_EINVAL, "variant argument %d outside 0..3", arg);
+    if (piece < 0 || piece % 16 != 0) return h->fail(SESNT_EINVAL, "piece size %d is not a multiple of 16 bytes", piece);
+    h->drop_graph();  // the graphs hold the launch arguments
+    h->variant = variant;
+    h->variant_arg = arg;
+    h->piece = piece;
+    return SESNT_OK;
+}
+
+int sesnt_element_kernel(const sesnt_t *h, char *name, int name_len, int choice[3]) {
+    if (!h || !name || name_len <= 0) return SESNT_EINVAL;
+    const char *n = h->dbl ? ops<double>(h)->element_name(h->args<double>(), h->sls, h->aniso)
+                           : ops<float>(h)->element_name(h->args<float>(), h->sls, h->aniso);
+    std::snprintf(name, (size_t)name_len, "%s", n);
+    if (choice) {
+        choice[0] = h->variant;
+        choice[1] = h->variant_arg;
+        choice[2] = h->piece;
+    }
+    return SESNT_OK;
 }
 
 int sesnt_info(const sesnt_t *h, long long out[6]) {

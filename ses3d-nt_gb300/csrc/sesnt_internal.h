@@ -47,6 +47,21 @@ struct SrcRec {
     int data[9];
 };
 
+// Element-kernel variants (StepArgs::variant). kVarAuto applies the launch
+// rules of launch_element; the others are chosen by the tuner
+// (sesnt_tune) or set by the caller (sesnt_set_element_variant) and fall
+// back to the rules where the handle's configuration has no such kernel.
+enum ElementVariant : int {
+    kVarAuto = 0,
+    kVarPoint = 1,       // k_element: one thread per element-local point
+    kVarPair = 2,        // k_element_pair: two simulations per thread (even-batch elastic)
+    kVarStage = 3,       // k_element_stage, state out by bulk store (SLS, degrees 4-7)
+    kVarStageReg = 4,    // k_element_stage, state out from registers
+    kVarPersistent = 5,  // k_element_tma: persistent, state by bulk copies
+    kVarColumns = 6,     // k_element_cols: one thread per column (elastic)
+    kVarCount
+};
+
 template <typename T>
 struct StepArgs {
     // grid
@@ -86,6 +101,9 @@ struct StepArgs {
     int pair;        // batched elastic steps: two simulations per thread (k_element_pair)
     int stage;       // SLS steps: state staged in shared memory by bulk copy (k_element_stage)
     int contraction; // element kernel contractions: 0 CUDA cores, 1 tensor cores TF32x3, 2 tensor cores BF16x3
+    int variant;     // ElementVariant
+    int variant_arg; // k_element_cols: index of the resident-block count (kColsMinb, 0..3)
+    int piece;       // bulk copies of a state unit in pieces of this many bytes (multiple of 16; 0: whole)
     T two_over_d[3]; // 2/dx_elm, 2/dy_elm, 2/dz_elm
     int *err;        // device error word (a bounded wait ran out)
     int wait_polls;  // bound of every device-side completion wait (mbarrier polls)
@@ -179,6 +197,8 @@ struct LpdOps {
     int (*derived)(const StepArgs<T> &, int which, int sim, const T *rot, T *loc, void *stream);
     // one-time kernel attributes (large dynamic shared memory)
     int (*prepare)();
+    // name of the element kernel a step launches with these arguments
+    const char *(*element_name)(const StepArgs<T> &, bool sls, bool aniso);
     int threads_element;
     size_t smem_element;
 };

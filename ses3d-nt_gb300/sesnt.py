@@ -34,6 +34,8 @@ FLAG_STRAIN = 32
 FLAG_ROTATION = 64
 FLAG_NO_PAIR = 128
 FLAG_NO_STAGE = 256
+FLAG_AUTOTUNE = 512
+ELEMENT_AUTO, ELEMENT_POINT, ELEMENT_PAIR, ELEMENT_STAGE, ELEMENT_STAGE_REG, ELEMENT_PERSISTENT, ELEMENT_COLUMNS = range(7)
 SOURCE_MT, SOURCE_SF = 0, 1
 WAVELETS = {"DELTA": 0, "RICKER": 1, "GAUSS": 2, "SIN**3": 3, "BRUNE": 4}
 CH_VX, CH_VY, CH_VZ, CH_N = 1, 2, 4, 8
@@ -160,6 +162,9 @@ def lib():
         "sesnt_get_field": (I, [P, I, I, P, I]),
         "sesnt_v_ptp": (I, [P, I, fp]),
         "sesnt_kinetic_energy": (I, [P, I, C.POINTER(C.c_double)]),
+        "sesnt_tune": (I, [P, C.c_char_p, I]),
+        "sesnt_set_element_variant": (I, [P, I, I, I]),
+        "sesnt_element_kernel": (I, [P, C.c_char_p, I, ip]),
         "sesnt_assemble_field": (I, [P, fp]),
         "sesnt_info": (I, [P, C.POINTER(C.c_longlong)]),
         "sesnt_footprint_bytes": (C.c_longlong, [G]),
@@ -372,6 +377,22 @@ class Simulation:
         out = np.zeros(2, np.float32)
         self._c(lib().sesnt_v_ptp(self._h, sim, _fptr(out)))
         return float(out[0]), float(out[1])
+
+    def tune(self):
+        """Tune the element kernel on this grid (after set_model, before stepping); returns the report."""
+        buf = C.create_string_buffer(8192)
+        self._c(lib().sesnt_tune(self._h, buf, len(buf)))
+        return buf.value.decode()
+
+    def set_element_variant(self, variant, arg=0, piece=8192):
+        self._c(lib().sesnt_set_element_variant(self._h, variant, arg, piece))
+
+    def element_kernel(self):
+        """(name of the element kernel a step launches, (variant, arg, piece))."""
+        buf = C.create_string_buffer(128)
+        ch = (C.c_int * 3)()
+        self._c(lib().sesnt_element_kernel(self._h, buf, len(buf), ch))
+        return buf.value.decode(), tuple(ch)
 
     def kinetic_energy(self, sim=0):
         """Kinetic energy of simulation `sim` in joules (elastic_vars.F90:218-246)."""

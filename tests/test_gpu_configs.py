@@ -6,16 +6,25 @@
   memory-variable fields against the FP32 oracle, each error also stated
   against the FP64 build of the same kernels. A shorter FP64 run checks the
   FP64 build against the FP64 oracle on the same grid.
-- The batched grid (64x64x32 elements, lpd 4, 3 SLS) with 4 of its seeded
-  sources in one batch, each simulation against its own oracle run. The
-  seeded positions and moment tensors are kept; the wavelets are shortened
-  to a width of 16 s (the grid's resolved period, 1/f_c) with onset 24 s so
-  that the pulse radiates within the 250 steps the oracle can afford here.
+- The batched grid (64x64x32 elements, lpd 4, 3 SLS) with 4 of its 64
+  seeded sources in one batch, each simulation against its own oracle run.
+  The 4 are the shallowest of the 64 (their positions and moment tensors
+  as seeded), with the wavelets shortened to a width of 16 s (the grid's
+  resolved period, 1/f_c) and onset 24 s, so that the pulse reaches the
+  surface receivers within the 250 steps the oracle can afford here; from
+  the deeper seeded sources (up to 300 km) nothing arrives in 25 s, and
+  relative errors of pre-arrival noise say nothing. The FP64 build of the
+  same batch is the anchor each error is also stated against.
 - The precision workload's generator (lpd 6, 3 SLS) on a 16x16x8 grid, dt
   0.15 s (Courant number 0.22 on this coarser grid), 1000 steps (150 s):
   the FP32 CUDA-core kernel, the Kahan-compensated update and the two
   tensor-core contraction variants against the FP32 oracle, and the FP64
-  build against the FP64 oracle.
+  build against the FP64 oracle. Seismograms over all 1000 steps;
+  wavefields at step 650 (97.5 s, the field's largest extent, just after the
+  wavelet's peak at 90 s). By step 1000 the taper has absorbed most of the
+  pulse, and there, as in any FP32 run of a decayed field, the relative
+  error of a wavefield is set by rounding (both the GPU and the oracle sit
+  near 1e-4 of FP64 there).
 
 Tolerances: 1e-4 relative L2 for FP32 results (the benchmark spec's bound), 1e-3
 for the BF16x3 contractions (a split into three bfloat16 products keeps about
@@ -118,59 +127,80 @@ def test_config2_full_grid_fp64_equals_fp64_oracle(gpu, sesnt_lib, oracle_mod):
 
 def test_config4_grid_batched_sources_match_oracle(gpu, sesnt_lib, oracle_mod):
     steps, batch = 250, 4
-    wl = workloads.config4(nt=steps, batch=batch)
-    for s in wl.sources:
-        s.width, s.onset = 16.0, 24.0
+    wl = workloads.config4(nt=steps)  # the 64 seeded sources
+    shallow = sorted(wl.sources, key=lambda x: x.depth)[:batch]
+    wl.grid.batch = batch
+    wl.sources = []
+    for q, src in enumerate(shallow):
+        src.sim, src.width, src.onset = q, 16.0, 24.0
+        wl.sources.append(src)
+    print("config4 grid: batch of the %d shallowest seeded sources, depths %s km"
+          % (batch, ", ".join("%.0f" % (x.depth / 1e3) for x in wl.sources)))
     g = gpu_run(wl, steps)
+    g64 = gpu_run(with_grid(wl, precision=8), steps)
     try:
-        seis = g.seismograms()
+        seis, seis64 = g.seismograms(), g64.seismograms()
         for s in range(batch):
             o = oracle_run(oracle_mod, wl, steps, sim=s)
             so = o.seismograms()
             assert np.abs(so).max() > 0
             e = rel_l2(seis[s], so)
-            print("config4 grid, batch member %d, %d steps: seismograms vs oracle %.2e" % (s, steps, e))
+            print("config4 grid, batch member %d, %d steps: seismograms GPU-FP32 vs oracle-FP32 %.2e, "
+                  "GPU-FP32 vs FP64 %.2e, oracle-FP32 vs FP64 %.2e"
+                  % (s, steps, e, rel_l2(seis[s], seis64[s]), rel_l2(so, seis64[s])))
             assert e < TOL
-            check_fields("config4 sim %d" % s, g, o, None,
+            check_fields("config4 sim %d" % s, g, o, g64,
                          {k: STATE[k] for k in ("vx", "vz", "sxz", "szz")} |
                          {k: MEMORY[k] for k in ("m0", "m8", "m17")}, TOL, sim=s)
             o.close()
     finally:
         g.close()
+        g64.close()
 
 
 def test_config3_generator_lpd6_variants_match_oracle(gpu, sesnt_lib, oracle_mod):
-    steps = 1000
+    steps, mid = 1000, 650
+    names = ("vx", "vz", "sxx", "syz")
     wl = workloads.config3(nt=steps, nx=16, ny=16, nz=8)
     wl.grid.dt = 0.15
-    o32 = oracle_run(oracle_mod, wl, steps)
-    o64 = oracle_run(oracle_mod, wl, steps, precision=8)
-    so, so64 = o32.seismograms(), o64.seismograms()
+
+    def oracle(precision):
+        o = oracle_mod.Oracle(wl.grid, precision)
+        oracle_mod.load_workload(o, wl)
+        o.run(mid)
+        f = {k: o.field(STATE[k]).astype(np.float64) for k in names}
+        o.run(steps - mid)
+        s = o.seismograms()
+        o.close()
+        return s, f
+
+    def gpu(grid):
+        with sesnt.Simulation(grid) as sim:
+            workloads.setup(sim, workloads.Workload(wl.name, grid, wl.model, wl.sources, wl.receivers))
+            sim.run(1, mid)
+            f = {k: sim.field(k, precision=8) for k in names}
+            sim.run(mid + 1, steps - mid)
+            return sim.seismograms()[0].astype(np.float64), f
+
+    so, fo = oracle(4)
+    so64, fo64 = oracle(8)
     assert np.abs(so).max() > 0
     print("config3 generator 16x16x8 lpd 6, %d steps: oracle-FP32 vs oracle-FP64 %.2e" % (steps, rel_l2(so, so64)))
-    g64 = gpu_run(with_grid(wl, precision=8), steps)
-    try:
-        e = rel_l2(g64.seismograms()[0].astype(np.float64), so64)
-        print("  FP64 build: seismograms vs FP64 oracle %.2e" % e)
-        assert e < 1e-6
-        for name in ("vx", "vz", "sxx", "syz"):
-            assert rel_l2(g64.field(name, precision=8), o64.field(STATE[name])) < 1e-10, name
-        variants = (("FP32", 0, TOL), ("Kahan", sesnt.FLAG_KAHAN, TOL), ("TF32x3", sesnt.FLAG_TC_TF32X3, TOL),
-                    ("BF16x3", sesnt.FLAG_TC_BF16X3, 1e-3))
-        for label, flags, tol in variants:
-            g = gpu_run(with_grid(wl, flags=flags), steps)
-            try:
-                s = g.seismograms()[0]
-                e, e64 = rel_l2(s, so), rel_l2(s, so64)
-                print("  %s: seismograms vs oracle-FP32 %.2e, vs FP64 %.2e" % (label, e, e64))
-                assert e < tol, label
-                for name in ("vx", "vz", "sxx"):
-                    ef = rel_l2(g.field(name, precision=8), o32.field(STATE[name]))
-                    print("  %s: final %s vs oracle-FP32 %.2e" % (label, name, ef))
-                    assert ef < tol, (label, name)
-            finally:
-                g.close()
-    finally:
-        g64.close()
-        o32.close()
-        o64.close()
+    s64, f64 = gpu(with_grid(wl, precision=8).grid)
+    e = rel_l2(s64, so64)
+    print("  FP64 build: seismograms vs FP64 oracle %.2e" % e)
+    assert e < 1e-6
+    for k in names:
+        assert rel_l2(f64[k], fo64[k]) < 1e-10, k
+    variants = (("FP32", 0, TOL), ("Kahan", sesnt.FLAG_KAHAN, TOL), ("TF32x3", sesnt.FLAG_TC_TF32X3, TOL),
+                ("BF16x3", sesnt.FLAG_TC_BF16X3, 1e-3))
+    for label, flags, tol in variants:
+        s, f = gpu(with_grid(wl, flags=flags).grid)
+        e, e64 = rel_l2(s, so), rel_l2(s, so64)
+        print("  %s: seismograms vs oracle-FP32 %.2e, vs FP64 %.2e" % (label, e, e64))
+        assert e < tol, label
+        for k in names:
+            ef = rel_l2(f[k], fo[k])
+            print("  %s: step-%d %s vs oracle-FP32 %.2e, vs FP64 %.2e, oracle-FP32 vs FP64 %.2e"
+                  % (label, mid, k, ef, rel_l2(f[k], f64[k]), rel_l2(fo[k], fo64[k])))
+            assert ef < tol, (label, k)

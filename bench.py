@@ -305,7 +305,7 @@ def run_ours(args):
                          % (info["algorithmic_bytes_per_step"] / 1e9),
                    "graph": not (g.flags & sesnt.FLAG_NO_GRAPH), "element": args.element,
                    "element_kernel": {"name": kname, "variant": choice[0], "arg": choice[1], "piece": choice[2],
-                                      "tuning": tune_report.strip().splitlines()[-1] if tune_report else None},
+                                      "tuning": tune_report.strip().splitlines()[1:] if tune_report else None},
                    "parallelism": "replicas" if WORLD > 1 else "single GPU"},
         "gpu_launches": graph_launches(K, info["launches_per_step"]),
         "clocks": clk,
@@ -366,8 +366,8 @@ def choose_element(sim, element):
 def timed_rate(wl, K, W, KP=0, element="tuned"):
     """Steps of one workload: W untimed, K timed with CUDA events on the
     library's stream, then KP steps with per-kernel events. Returns
-    (GLL-point-updates/s, ms/step, info, element-kernel ms per step or None,
-    element kernel name)."""
+    (GLL-point-updates/s, ms/step, info, per-step ms of the element, source,
+    node and receiver kernels or None, element kernel name)."""
     import sesnt
     import workloads
     g = wl.grid
@@ -379,8 +379,8 @@ def timed_rate(wl, K, W, KP=0, element="tuned"):
         sim.run(1, W)
         sim.synchronize()
         ms = sim.run_timed(W + 1, K)
-        el = float(sim.run_profiled(W + K + 1, KP)[0]) / KP if KP > 0 else None
-    return g.n_loc * K * g.batch / (ms / 1e3), ms / K, info, el, kname
+        prof = [float(x) / KP for x in sim.run_profiled(W + K + 1, KP)] if KP > 0 else None
+    return g.n_loc * K * g.batch / (ms / 1e3), ms / K, info, prof, kname
 
 
 def batched_headline(args):
@@ -408,7 +408,8 @@ def batched_headline(args):
             wl.sources = workloads.random_sources(wl.grid, 64, np.random.Generator(np.random.PCG64(1)))
         else:
             wl = make(nt)
-        rate, ms, info, t_el, kname = timed_rate(wl, K, W, KP)
+        rate, ms, info, prof, kname = timed_rate(wl, K, W, KP)
+        t_el = prof[0]
         plain = copy.copy(wl)
         plain.grid = copy.copy(wl.grid)
         plain.grid.batch = 1
@@ -429,6 +430,11 @@ def batched_headline(args):
                            % (pinfo["algorithmic_bytes_per_step"] / 1e6)},
             "vs_plain": rate / prate,
             "element_kernel_ms": t_el, "element_kernel_hbm_frac": el_frac, "step_hbm_frac": step_frac,
+            "node_kernel_ms": prof[2],
+            # the replayed step's time outside the two kernels on its critical path (the source and
+            # receiver kernels overlap them on a side stream): all that one persistent launch over
+            # steps could remove
+            "outside_kernels_frac": 1.0 - (prof[0] + prof[2]) / ms,
             "target_met": bool(rate / prate >= 2.0 and step_frac >= 0.7),
         }
     return out

@@ -80,6 +80,7 @@ extern "C" {
 #define SESNT_ELEMENT_COLUMNS 6     /* one thread per (i, j) column of an element (elastic); arg
                                        selects the resident blocks per SM the kernel is sized for
                                        (0: 4, 1: 5, 2: 6, 3: 8) */
+#define SESNT_ELEMENT_COLUMNS_STAGED 7 /* the same with each block's stress staged by bulk copy */
 
 /* source kinds (sesnt_add_source) */
 #define SESNT_SOURCE_MT 0 /* moment tensor: comp = Mxx Mxy Mxz Myy Myz Mzz */
@@ -245,7 +246,7 @@ int sesnt_synchronize(sesnt_t *h);
 /* No counterpart in the reference. Tunes the element kernel on this handle's
  * grid, precision and batch: times every variant that computes this step
  * (one point per thread, paired simulations, one thread per column at four
- * register budgets, the staged kernel with bulk or register stores and
+ * register budgets with the stress loaded per point or staged per block, the staged kernel with bulk or register stores and
  * 0/4/8/16 KB copy pieces, the persistent kernel) with CUDA events on the
  * handle's stream, keeps the fastest and appends it to the tuning cache
  * ($SESNT_TUNE_CACHE, else $HOME/.cache/sesnt-tune.txt), keyed by GPU name,

@@ -26,16 +26,52 @@ struct ColCfg {
     static constexpr int G = PP <= 128 ? 128 / PP : 1;
     static constexpr int NT = ((G * PP + 31) / 32) * 32;
     static constexpr size_t SMEM_T = 4 * PP + (size_t)G * 9 * NP;  // values of T: tables, v + x/y fluxes
+    static constexpr int NPS = state_stride(NP);
+    // STAGE: the stress of the block's G units (one contiguous range of the
+    // element-major state) follows, 128-byte aligned, then the mbarrier
+    template <typename T>
+    SESNT_HD static constexpr size_t stage_offset() { return ((sizeof(T) * SMEM_T + 127) / 128) * 128; }
+    template <typename T>
+    SESNT_HD static constexpr size_t smem(bool stage) {
+        return stage ? stage_offset<T>() + sizeof(T) * (size_t)G * 6 * NPS + 16 : sizeof(T) * SMEM_T;
+    }
 };
 
-template <int N, typename T, bool ANISO, int MINB>
+// STAGE: thread 0 bulk-copies the block's stress range (G units of 6 x NPS
+// values, contiguous and 16-byte aligned) into shared memory at the start,
+// under one mbarrier with a bounded wait; the points read and write their
+// stress there and thread 0 bulk-stores the range after the flux barrier.
+// Without it each point loads its stress from global memory one point of the
+// column ahead.
+template <int N, typename T, bool ANISO, int MINB, bool STAGE>
 __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols(const StepArgs<T> a) {
     using C = ColCfg<N>;
     constexpr int P = C::P, PP = C::PP, NP = C::NP, G = C::G, NT = C::NT;
-    constexpr int NPS = state_stride(NP);
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int NPS = C::NPS;
+    extern __shared__ __align__(128) unsigned char cols_smem_raw[];
+    unsigned char *smem_raw = cols_smem_raw;
     T *sD = reinterpret_cast<T *>(smem_raw);  // [4][P*P]: Dx Dy Dz (scaled) | Dt
     const int t = threadIdx.x;
+    const long long units = (long long)a.nel * a.S;
+    const long long ufirst = (long long)blockIdx.x * G;
+    const int nunits = (int)(units - ufirst < G ? units - ufirst : G);  // units of this block
+    T *stage = reinterpret_cast<T *>(smem_raw + C::template stage_offset<T>());
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(smem_raw + C::template stage_offset<T>() +
+                                                  sizeof(T) * (size_t)G * 6 * NPS);
+    const uint32_t stage_bytes = (uint32_t)(sizeof(T) * (size_t)nunits * 6 * NPS);  // a multiple of 16
+    bool issued = false;
+    if constexpr (STAGE) {
+        if (t == 0) {
+            const uint32_t mb = tma_smem(mbar);
+            tma_mbar_init(mb);
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+            if (!a.drop_completion && in_range((size_t)(ufirst + nunits) * 6 * NPS - 1, (size_t)units * 6 * NPS, a.err)) {
+                tma_expect(mb, stage_bytes);
+                tma_load_unit(stage, a.sig + (size_t)ufirst * 6 * NPS, stage_bytes, mb, a.piece);
+                issued = true;
+            }
+        }
+    }
     for (int x = t; x < 4 * PP; x += NT) sD[x] = a.tabD[x];
     const int gl = t / PP;
     const int c = t - gl * PP;
@@ -43,8 +79,7 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols(const Step
     T *sv = sD + 4 * PP + (size_t)gl * 9 * NP;  // this unit's [3][NP] velocity slab
     T *sx = sv + 3 * NP;                        // [3][NP] x fluxes (xx, xy, xz weighted)
     T *sy = sx + 3 * NP;                        // [3][NP] y fluxes
-    const long long units = (long long)a.nel * a.S;
-    const long long unit = (long long)blockIdx.x * G + gl;
+    const long long unit = ufirst + gl;
     const size_t nuni = (size_t)a.nuni, nloc = (size_t)a.nloc;
     int e = 0, s = 0, ex = 0, ey = 0, ez = 0;
     bool act = gl < G && unit < units;
@@ -61,7 +96,8 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols(const Step
     const size_t kstep = (size_t)a.NXU * a.NYU;  // unique-index stride of k
     const size_t u0 = act ? unique_index<N>(a.NXU, a.NYU, ex, ey, ez, i, j, 0) : 0;
     const size_t l0 = (size_t)e * NP + c;        // element-local index of (i, j, 0)
-    T *sig = a.sig + (size_t)unit * 6 * NPS + c;
+    // this column's stress at k = 0: the staged copy or global memory
+    T *sig = STAGE ? stage + (size_t)gl * 6 * NPS + c : a.sig + (size_t)unit * 6 * NPS + c;
     T vc[3][P];  // this column's velocity
     if (act) {
         const T *vs = a.v + (size_t)s * 3 * nuni;
@@ -90,11 +126,15 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols(const Step
             B = ld_stream(a.B + li);
             Cc = ld_stream(a.C + li);
         }
+        if constexpr (!STAGE) {
 #pragma unroll
-        for (int q = 0; q < 6; ++q) sgk[q] = ld_stream(sig + q * NPS + PP * k);
+            for (int q = 0; q < 6; ++q) sgk[q] = ld_stream(sig + q * NPS + PP * k);
+        }
     };
     if (act) load_point(0, lam, mu, cA, cB, cC, sg);
-    __syncthreads();  // tables and velocity slabs
+    __syncthreads();  // tables, velocity slabs and the mbarrier's initialisation
+    bool landed = true;
+    if constexpr (STAGE) landed = tma_try_wait(tma_smem(mbar), 0, a.wait_polls);
     const T *Dx = sD, *Dy = sD + PP, *Dz = sD + 2 * PP, *Dt = sD + 3 * PP;
     T dxi[P], dyj[P];
 #pragma unroll
@@ -108,7 +148,11 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols(const Step
     for (int k = 0; k < P; ++k) {
         T nlam = 0, nmu = 0, nA = 0, nB = 0, nC = 0, nsg[6] = {0, 0, 0, 0, 0, 0};
         if (k + 1 < P && act) load_point(k + 1, nlam, nmu, nA, nB, nC, nsg);
-        if (act) {
+        if constexpr (STAGE) {
+#pragma unroll
+            for (int q = 0; q < 6; ++q) sg[q] = act && landed ? sig[q * NPS + PP * k] : T(0);
+        }
+        if (act && landed) {
             T ev[9];
 #pragma unroll
             for (int x = 0; x < 9; ++x) ev[x] = 0;
@@ -128,8 +172,9 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols(const Step
                 ev[8] += vc[2][q] * dz;
             }
             T sn[6], gw[3];
-            point_stress<N, T, 0, ANISO>(a, ev, vc[0][k], vc[1][k], vc[2][k], i, j, k, ex, ey, ez, lam, mu, T(0), cA,
-                                         cB, cC, sg, m0, sig + PP * k, nullptr, NPS, nloc, nullptr, sn, gw);
+            point_stress<N, T, 0, ANISO, false, STAGE>(a, ev, vc[0][k], vc[1][k], vc[2][k], i, j, k, ex, ey, ez, lam,
+                                                       mu, T(0), cA, cB, cC, sg, m0, sig + PP * k, nullptr, NPS, nloc,
+                                                       nullptr, sn, gw);
             const int p = c + PP * k;
             sx[p] = sn[0] * gw[0];
             sx[NP + p] = sn[1] * gw[0];
@@ -149,71 +194,96 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols(const Step
 #pragma unroll
         for (int q = 0; q < 6; ++q) sg[q] = nsg[q];
     }
-    __syncthreads();  // x and y flux slabs
-    if (!act) return;
-    T dti[P], dtj[P];
-#pragma unroll
-    for (int q = 0; q < P; ++q) {
-        dti[q] = Dt[i * P + q];
-        dtj[q] = Dt[j * P + q];
-    }
-    T *F = a.F + (size_t)s * 3 * nuni;
-#pragma unroll
-    for (int k = 0; k < P; ++k) {
-        T fx = 0, fy = 0, fz = 0;
-        const T *row = sx + P * (j + P * k);
-        const T *col = sy + i + PP * k;
+    // weak divergence of this column's points and their assembly
+    auto column_divergence = [&]() {
+        T dti[P], dtj[P];
 #pragma unroll
         for (int q = 0; q < P; ++q) {
-            const T di = dti[q], dj = dtj[q], dk = Dt[k * P + q];
-            fx += zf[0][q] * dk + col[P * q] * dj + row[q] * di;
-            fy += zf[1][q] * dk + col[NP + P * q] * dj + row[NP + q] * di;
-            fz += zf[2][q] * dk + col[2 * NP + P * q] * dj + row[2 * NP + q] * di;
+            dti[q] = Dt[i * P + q];
+            dtj[q] = Dt[j * P + q];
         }
-        const size_t u = u0 + k * kstep;
-        atomicAdd(F + u, fx);
-        atomicAdd(F + nuni + u, fy);
-        atomicAdd(F + 2 * nuni + u, fz);
+        T *F = a.F + (size_t)s * 3 * nuni;
+#pragma unroll
+        for (int k = 0; k < P; ++k) {
+            T fx = 0, fy = 0, fz = 0;
+            const T *row = sx + P * (j + P * k);
+            const T *col = sy + i + PP * k;
+#pragma unroll
+            for (int q = 0; q < P; ++q) {
+                const T di = dti[q], dj = dtj[q], dk = Dt[k * P + q];
+                fx += zf[0][q] * dk + col[P * q] * dj + row[q] * di;
+                fy += zf[1][q] * dk + col[NP + P * q] * dj + row[NP + q] * di;
+                fz += zf[2][q] * dk + col[2 * NP + P * q] * dj + row[2 * NP + q] * di;
+            }
+            const size_t u = u0 + k * kstep;
+            atomicAdd(F + u, fx);
+            atomicAdd(F + nuni + u, fy);
+            atomicAdd(F + 2 * nuni + u, fz);
+        }
+    };
+    // updated stress in the stage: visible to the bulk-copy engine after the barrier
+    if constexpr (STAGE) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    const bool ok = __syncthreads_and(landed) != 0;  // x and y flux slabs
+    if constexpr (STAGE) {
+        if (t == 0) {
+            if (ok) {
+                tma_store(a.sig + (size_t)ufirst * 6 * NPS, tma_smem(stage), stage_bytes);
+                tma_commit();
+            } else {
+                atomicExch(a.err, 1);
+                // the copy may still be in flight: one more bounded wait
+                // before the block's shared memory is released
+                if (issued) tma_try_wait(tma_smem(mbar), 0, a.wait_polls);
+            }
+        }
     }
+    if (act && ok) column_divergence();
+    if constexpr (STAGE)
+        if (ok && t == 0) tma_wait_read<0>();  // the store has read the stage before it is released
 }
+
 
 // Resident blocks per SM the column kernel is sized for (FP32); FP64 uses 1
 // (as k_element). Selected per grid by the tuner among the instantiated
 // values.
 constexpr int kColsMinb[] = {4, 5, 6, 8};
 
-template <int N, typename T, bool ANISO, int MINB>
+template <int N, typename T, bool ANISO, int MINB, bool STAGE>
 int launch_element_cols_m(const StepArgs<T> &a, void *stream) {
     using C = ColCfg<N>;
     const long long units = (long long)a.nel * a.S;
-    const size_t smem = sizeof(T) * C::SMEM_T;
+    const size_t smem = C::template smem<T>(STAGE);
     if (smem > kMaxSmemPerBlock) return 1;
-    k_element_cols<N, T, ANISO, MINB><<<(unsigned)((units + C::G - 1) / C::G), C::NT, smem, (cudaStream_t)stream>>>(a);
+    k_element_cols<N, T, ANISO, MINB, STAGE>
+        <<<(unsigned)((units + C::G - 1) / C::G), C::NT, smem, (cudaStream_t)stream>>>(a);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
 
 // minb_idx selects kColsMinb[] (FP32); returns 1 if this configuration has
 // no column kernel (the caller falls back).
-template <int N, typename T, bool ANISO>
+template <int N, typename T, bool ANISO, bool STAGE>
 int launch_element_cols(const StepArgs<T> &a, int minb_idx, void *stream) {
     if constexpr (sizeof(T) == 8) {
-        return launch_element_cols_m<N, T, ANISO, 1>(a, stream);
+        return launch_element_cols_m<N, T, ANISO, 1, STAGE>(a, stream);
     } else {
         switch (minb_idx) {
-            case 0: return launch_element_cols_m<N, T, ANISO, kColsMinb[0]>(a, stream);
-            case 1: return launch_element_cols_m<N, T, ANISO, kColsMinb[1]>(a, stream);
-            case 2: return launch_element_cols_m<N, T, ANISO, kColsMinb[2]>(a, stream);
-            default: return launch_element_cols_m<N, T, ANISO, kColsMinb[3]>(a, stream);
+            case 0: return launch_element_cols_m<N, T, ANISO, kColsMinb[0], STAGE>(a, stream);
+            case 1: return launch_element_cols_m<N, T, ANISO, kColsMinb[1], STAGE>(a, stream);
+            case 2: return launch_element_cols_m<N, T, ANISO, kColsMinb[2], STAGE>(a, stream);
+            default: return launch_element_cols_m<N, T, ANISO, kColsMinb[3], STAGE>(a, stream);
         }
     }
 }
 
 template <int N, typename T, bool ANISO, int MINB>
 int prepare_element_cols_m() {
-    const size_t smem = sizeof(T) * ColCfg<N>::SMEM_T;
-    if (smem <= 48 * 1024 || smem > kMaxSmemPerBlock) return 0;
-    return cudaFuncSetAttribute(k_element_cols<N, T, ANISO, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)smem) == cudaSuccess ? 0 : -1;
+    for (bool stage : {false, true}) {
+        const size_t smem = ColCfg<N>::template smem<T>(stage);
+        if (smem <= 48 * 1024 || smem > kMaxSmemPerBlock) continue;
+        auto f = stage ? k_element_cols<N, T, ANISO, MINB, true> : k_element_cols<N, T, ANISO, MINB, false>;
+        if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) return -1;
+    }
+    return 0;
 }
 
 template <int N, typename T, bool ANISO>

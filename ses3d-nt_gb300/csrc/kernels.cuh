@@ -949,9 +949,9 @@ int prepare_variant() {
 
 }  // namespace sesnt
 
-#include "element_cols.cuh"
 #include "element_tc.cuh"
 #include "element_tma.cuh"
+#include "element_cols.cuh"
 
 namespace sesnt {
 
@@ -985,7 +985,7 @@ int launch_element_bulk(const StepArgs<T> &a, bool sls, bool aniso, void *stream
 // The element kernel one step launches, decided on the host from the
 // handle's configuration (plan_element) so that the launcher, the tuner and
 // the kernel name a caller reads agree.
-enum class ElemKernel : int { Tc, Point, Pair, StageBulk, StageReg, Persistent, Columns };
+enum class ElemKernel : int { Tc, Point, Pair, StageBulk, StageReg, Persistent, Columns, ColumnsStaged };
 
 inline const char *elem_kernel_name(ElemKernel k) {
     switch (k) {
@@ -996,6 +996,7 @@ inline const char *elem_kernel_name(ElemKernel k) {
         case ElemKernel::StageReg: return "k_element_stage (register stores)";
         case ElemKernel::Persistent: return "k_element_tma";
         case ElemKernel::Columns: return "k_element_cols";
+        case ElemKernel::ColumnsStaged: return "k_element_cols (staged stress)";
     }
     return "?";
 }
@@ -1018,8 +1019,8 @@ constexpr bool has_staged() {
 }
 
 template <int N, typename T>
-constexpr bool has_columns() {
-    return sizeof(T) * ColCfg<N>::SMEM_T <= kMaxSmemPerBlock;
+constexpr bool has_columns(bool stage) {
+    return ColCfg<N>::template smem<T>(stage) <= kMaxSmemPerBlock;
 }
 
 // A variant chosen by the tuner or the caller (StepArgs::variant) where the
@@ -1039,7 +1040,8 @@ ElemKernel plan_element(const StepArgs<T> &a, bool sls, bool aniso) {
         case kVarStage: if (sls && has_staged<N, T>()) return ElemKernel::StageBulk; break;
         case kVarStageReg: if (sls && has_staged<N, T>()) return ElemKernel::StageReg; break;
         case kVarPersistent: if (has_persistent<N, T>(sls, aniso)) return ElemKernel::Persistent; break;
-        case kVarColumns: if (!sls && has_columns<N, T>()) return ElemKernel::Columns; break;
+        case kVarColumns: if (!sls && has_columns<N, T>(false)) return ElemKernel::Columns; break;
+        case kVarColumnsStaged: if (!sls && has_columns<N, T>(true)) return ElemKernel::ColumnsStaged; break;
         default: break;
     }
     if (a.persistent && has_persistent<N, T>(sls, aniso)) return ElemKernel::Persistent;
@@ -1076,8 +1078,13 @@ int launch_element(const StepArgs<T> &a, bool sls, bool aniso, void *stream) {
             }
             return -1;
         case ElemKernel::Columns: {
-            const int r = aniso ? launch_element_cols<N, T, true>(a, a.variant_arg, stream)
-                                : launch_element_cols<N, T, false>(a, a.variant_arg, stream);
+            const int r = aniso ? launch_element_cols<N, T, true, false>(a, a.variant_arg, stream)
+                                : launch_element_cols<N, T, false, false>(a, a.variant_arg, stream);
+            return r > 0 ? -1 : r;
+        }
+        case ElemKernel::ColumnsStaged: {
+            const int r = aniso ? launch_element_cols<N, T, true, true>(a, a.variant_arg, stream)
+                                : launch_element_cols<N, T, false, true>(a, a.variant_arg, stream);
             return r > 0 ? -1 : r;
         }
         case ElemKernel::Pair: b.pair = 1; break;

@@ -387,10 +387,7 @@ struct sesnt_handle {
     // Whether an element kernel of this handle has bounded device-side waits
     // (tensor-core, persistent bulk-copy, or the staged SLS kernel of degrees
     // 4-7), i.e. whether the error word can be set without the bounds check.
-    bool bounded_waits() const {
-        if (g.flags & (SESNT_FLAG_TC_TF32X3 | SESNT_FLAG_TC_BF16X3 | SESNT_FLAG_PERSISTENT_ELEMENT)) return true;
-        return sls && g.lpd >= 4 && !(g.flags & (SESNT_FLAG_NO_STAGE | SESNT_FLAG_STRAIN));
-    }
+    bool bounded_waits() const;
     int wait_status() {
 #ifndef SESNT_BOUNDS_CHECK
         if (!bounded_waits()) return SESNT_OK;
@@ -649,6 +646,15 @@ int setup_tables(sesnt_t *h) {
 template <typename T>
 const LpdOps<T> *ops(const sesnt_t *h) {
     return lpd_ops<T>(h->N);
+}
+
+// Whether the element kernel a step launches has bounded device-side waits
+// (the staged, persistent, tensor-core and staged-column kernels), i.e.
+// whether the error word can be set without the bounds check.
+bool sesnt_handle::bounded_waits() const {
+    const char *n = dbl ? ops<double>(this)->element_name(args<double>(), sls, aniso)
+                        : ops<float>(this)->element_name(args<float>(), sls, aniso);
+    return std::strstr(n, "stage") || std::strstr(n, "_tma") || std::strstr(n, "_tc");
 }
 
 int zero_state(sesnt_t *h) {
@@ -1438,7 +1444,8 @@ struct TuneChoice {
 // Candidates for this handle: every element kernel that computes this step
 // (tensor-core contractions change the arithmetic and are never chosen):
 // one point per thread; paired simulations (even elastic batches); one
-// thread per column at each instantiated resident-block count (elastic);
+// thread per column at each instantiated resident-block count, with the
+// stress loaded per point or staged per block (elastic);
 // the staged kernel with bulk or register stores and four piece sizes (SLS);
 // the persistent kernel.
 std::vector<TuneChoice> tune_candidates(const sesnt_t *h) {
@@ -1446,6 +1453,7 @@ std::vector<TuneChoice> tune_candidates(const sesnt_t *h) {
     if (!h->sls) {
         if (h->S % 2 == 0) c.push_back({kVarPair, 0, 8192});
         for (int m = 0; m < 4; ++m) c.push_back({kVarColumns, m, 8192});
+        for (int m = 0; m < 4; ++m) c.push_back({kVarColumnsStaged, m, 0});
     } else {
         for (int v : {kVarStage, kVarStageReg})
             for (int piece : {0, 4096, 8192, 16384}) c.push_back({v, 0, piece});
@@ -1531,7 +1539,8 @@ int tune_impl(sesnt_t *h, TuneChoice *best_out, double *best_ms) {
                                 (c.variant == kVarStage && name == "k_element_stage") ||
                                 (c.variant == kVarStageReg && name == "k_element_stage (register stores)") ||
                                 (c.variant == kVarPersistent && name == "k_element_tma") ||
-                                (c.variant == kVarColumns && name == "k_element_cols");
+                                (c.variant == kVarColumns && name == "k_element_cols") ||
+                                (c.variant == kVarColumnsStaged && name == "k_element_cols (staged stress)");
         if (!applicable) continue;
         auto launch = [&](int n) {
             for (int q = 0; q < n; ++q)

@@ -59,6 +59,7 @@ enum ElementVariant : int {
     kVarStageReg = 4,    // k_element_stage, state out from registers
     kVarPersistent = 5,  // k_element_tma: persistent, state by bulk copies
     kVarColumns = 6,     // k_element_cols: one thread per column (elastic)
+    kVarColumnsStaged = 7,  // k_element_cols with the block's stress staged by bulk copy
     kVarCount
 };
 

@@ -51,14 +51,37 @@ def test_column_kernel_matches_point_kernel(gpu, sesnt_lib, lpd, precision):
         wl = batch_of(with_grid(small_workload(lpd, aniso=aniso, nt=120), precision=precision), batch)
         sp, vp, name_p, _, _ = run(wl, 120, sesnt.ELEMENT_POINT)
         assert name_p == "k_element"
-        for arg in ((0, 1, 2, 3) if precision == 4 else (0,)):
-            sc, vcol, name_c, choice, _ = run(wl, 120, sesnt.ELEMENT_COLUMNS, arg)
-            assert name_c == "k_element_cols" and choice[:2] == (sesnt.ELEMENT_COLUMNS, arg)
-            e, ev = rel_l2(sc, sp), rel_l2(vcol, vp)
-            print("lpd %d prec %d aniso %d batch %d arg %d: columns vs point seismograms %.2e, vz %.2e"
-                  % (lpd, precision, aniso, batch, arg, e, ev))
-            assert np.abs(sp).max() > 0
-            assert e < tol and ev < tol
+        for variant, kname in ((sesnt.ELEMENT_COLUMNS, "k_element_cols"),
+                               (sesnt.ELEMENT_COLUMNS_STAGED, "k_element_cols (staged stress)")):
+            for arg in ((0, 1, 2, 3) if precision == 4 else (0,)):
+                sc, vcol, name_c, choice, _ = run(wl, 120, variant, arg, piece=0 if arg % 2 else 4096)
+                assert name_c == kname and choice[:2] == (variant, arg)
+                e, ev = rel_l2(sc, sp), rel_l2(vcol, vp)
+                print("lpd %d prec %d aniso %d batch %d %s arg %d: columns vs point seismograms %.2e, vz %.2e"
+                      % (lpd, precision, aniso, batch, kname, arg, e, ev))
+                assert np.abs(sp).max() > 0
+                assert e < tol and ev < tol
+
+
+def test_staged_column_wait_runs_out_and_reports(gpu, sesnt_lib):
+    """The staged column kernel's one mbarrier wait per block is bounded:
+    with its bulk load dropped the wait runs out, synchronising returns
+    SESNT_ETIMEOUT, and after sesnt_reset the handle steps normally again."""
+    wl = batch_of(small_workload(4, nt=40), 2)
+    with sesnt.Simulation(wl.grid) as sim:
+        workloads.setup(sim, wl)
+        sim.set_element_variant(sesnt.ELEMENT_COLUMNS_STAGED, 0, 0)
+        sim.set_wait_limit(64, drop_completion=True)
+        sim.run(1, 2)
+        with pytest.raises(sesnt.SesntError) as e:
+            sim.synchronize()
+        assert e.value.code == sesnt.ETIMEOUT
+        sim.set_wait_limit(1 << 22)
+        sim.reset()
+        sim.run(1, 40)
+        again = sim.seismograms()
+    fresh, _, _, _, _ = run(wl, 40, sesnt.ELEMENT_POINT)
+    assert rel_l2(again, fresh) < 1e-5
 
 
 def test_column_kernel_matches_oracle(gpu, sesnt_lib, oracle_mod):

@@ -648,6 +648,8 @@ const LpdOps<T> *ops(const sesnt_t *h) {
     return lpd_ops<T>(h->N);
 }
 
+}  // namespace
+
 // Whether the element kernel a step launches has bounded device-side waits
 // (the staged, persistent, tensor-core and staged-column kernels), i.e.
 // whether the error word can be set without the bounds check.
@@ -656,6 +658,8 @@ bool sesnt_handle::bounded_waits() const {
                         : ops<float>(this)->element_name(args<float>(), sls, aniso);
     return std::strstr(n, "stage") || std::strstr(n, "_tma") || std::strstr(n, "_tc");
 }
+
+namespace {
 
 int zero_state(sesnt_t *h) {
     const size_t E = h->esize;

@@ -226,8 +226,10 @@ def element_kernel_name(element, g):
     --element choice other than tuned/columns (kernels.cuh:plan_element); a
     run reads the kernel it actually launched from the library."""
     import sesnt
-    if element == "columns":
-        return "k_element_cols" if g.n_sls == 0 else element_kernel_name("simple", g)
+    if element.startswith("columns"):
+        if g.n_sls:
+            return element_kernel_name("simple", g)
+        return "k_element_cols (staged stress)" if element.startswith("columns_staged") else "k_element_cols"
     if element.startswith("tc_"):
         return "k_element_tc"
     if element == "persistent":
@@ -358,8 +360,10 @@ def choose_element(sim, element):
     import sesnt
     if element == "tuned":
         return sim.tune()
-    if element == "columns":
-        sim.set_element_variant(sesnt.ELEMENT_COLUMNS, 0)
+    if element.startswith("columns"):
+        arg = int(element.split(":")[1]) if ":" in element else 0
+        v = sesnt.ELEMENT_COLUMNS_STAGED if element.startswith("columns_staged") else sesnt.ELEMENT_COLUMNS
+        sim.set_element_variant(v, arg, 0)
     return None
 
 
@@ -640,7 +644,8 @@ def main():
     ap.add_argument("--no-batched", dest="batched", action="store_false",
                     help="skip the batched-against-plain comparison of the default run")
     ap.add_argument("--element", default="tuned",
-                    choices=["tuned", "simple", "columns", "persistent", "unstaged", "tc_tf32x3", "tc_bf16x3"],
+                    choices=["tuned", "simple", "persistent", "unstaged", "tc_tf32x3", "tc_bf16x3"] +
+                            ["columns:%d" % q for q in range(4)] + ["columns_staged:%d" % q for q in range(4)],
                     help="element kernel variant (all compute the full step): tuned = the library's tuner "
                          "picks on this grid; simple = the launch rules; tc_*: tcgen05 contractions")
     args = ap.parse_args()

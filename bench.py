@@ -391,8 +391,10 @@ def batched_headline(args):
     """The batched form against the plain one-source step on the same grid
     and model: 64 simulations (one per seeded source) in one handle, whose
     steps read the shared material, metric and mass once per element block,
-    against one simulation. Two grids: the batched workload's own (64x64x32,
-    lpd 4, 3 SLS) and the plain workload's (12x12x8, lpd 4, elastic). For
+    against one simulation. Three grids: the batched workload's own
+    (64x64x32, lpd 4, 3 SLS), the plain workload's (12x12x8, lpd 4, elastic)
+    and the served workload's smallest request (16x16x8, lpd 4, 3 SLS, 32
+    sources). For
     each: the batched and plain rates, their ratio, the batched element
     kernel's algorithmic bytes over its event-timed duration as a fraction
     of the measured HBM bandwidth, and the whole step's algorithmic bytes over
@@ -402,16 +404,25 @@ def batched_headline(args):
     import workloads
     hbm, peak_kind = peaks()
     out = {"peak_gbs": hbm, "peak_source": peak_kind, "target": {"vs_plain": 2.0, "hbm_frac": 0.7}}
+    def config1_grid(nt):
+        wl = workloads.config1(nt=nt)
+        wl.grid.batch = 64
+        wl.sources = workloads.random_sources(wl.grid, 64, np.random.Generator(np.random.PCG64(1)))
+        return wl
+
+    def smallest_request(nt):
+        # the served workload's smallest request shape: 16x16 lateral and 8 radial elements,
+        # lpd 4, 3 SLS, the config-2 model generator, its largest source count (32)
+        wl = workloads.config4(nt=nt, batch=32, nx=16, ny=16, nz=8)
+        wl.name = "served_smallest_request_32src_16x16x8_lpd4"
+        return wl
+
     cases = (("config4_batched_64src_64x64x32_lpd4", lambda nt: workloads.config4(nt=nt), 4, 2, 3),
-             ("config1_grid_batched_64src_12x12x8_lpd4", None, 100, 5, 10))
+             ("config1_grid_batched_64src_12x12x8_lpd4", config1_grid, 100, 5, 10),
+             ("served_smallest_request_32src_16x16x8_lpd4", smallest_request, 100, 5, 10))
     for name, make, K, W, KP in cases:
-        nt = W + K + KP + 1
-        if make is None:
-            wl = workloads.config1(nt=max(nt, 400 + 16))
-            wl.grid.batch = 64
-            wl.sources = workloads.random_sources(wl.grid, 64, np.random.Generator(np.random.PCG64(1)))
-        else:
-            wl = make(nt)
+        nt = max(W + K + KP + 1, 416)
+        wl = make(nt)
         rate, ms, info, prof, kname = timed_rate(wl, K, W, KP)
         t_el = prof[0]
         plain = copy.copy(wl)
@@ -419,7 +430,7 @@ def batched_headline(args):
         plain.grid.batch = 1
         plain.sources = [copy.copy(wl.sources[0])]
         plain.sources[0].sim = 0
-        Kp = 400 if make is None else 40
+        Kp = 40 if wl.grid.n_loc * wl.grid.batch > 1e9 else 400
         plain.grid.nt = max(plain.grid.nt, 5 + Kp + 1)
         prate, pms, pinfo, _, pname = timed_rate(plain, Kp, 5)
         eb = element_kernel_bytes(wl.grid)

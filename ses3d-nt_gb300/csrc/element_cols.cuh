@@ -25,15 +25,32 @@ struct ColCfg {
     // units per block: as many whole columns sets as fit 128 threads
     static constexpr int G = PP <= 128 ? 128 / PP : 1;
     static constexpr int NT = ((G * PP + 31) / 32) * 32;
-    static constexpr size_t SMEM_T = 4 * PP + (size_t)G * 9 * NP;  // values of T: tables, v + x/y fluxes
+    // Shared-memory stride of one unit's slabs (v, x fluxes, y fluxes:
+    // 9 x NP values), padded so that it is congruent to PP modulo the 32
+    // banks: thread t = unit*PP + c then finds the element c of its unit's
+    // slab in bank t mod 32 (for 4-byte values), and the two units a warp
+    // spans never meet in a bank on the stores, the y-line loads or the
+    // x-line loads. Unpadded (9*125 = 1125 = 5 mod 32 at degree 4) a third
+    // of the shared-memory wavefronts were bank conflicts.
+    static constexpr int US = 9 * NP + ((PP - 9 * NP) % 32 + 32) % 32;
+    static constexpr size_t SMEM_T = 4 * PP + (size_t)G * US;  // values of T: tables, slabs
     static constexpr int NPS = state_stride(NP);
     // STAGE: the stress of the block's G units (one contiguous range of the
-    // element-major state) follows, 128-byte aligned, then the mbarrier
+    // element-major state, 6 x NPS values per unit) follows, 128-byte
+    // aligned, one unit every SS values, then the mbarrier. SS is padded to
+    // a multiple of 16 bytes near PP modulo 32 banks (the same reason as US;
+    // 6 x 128 = 0 mod 32 at degree 4 put every unit's column c in one bank).
+    template <typename T>
+    SESNT_HD static constexpr int stage_stride() {
+        constexpr int q = 16 / (int)sizeof(T);  // values per 16 bytes
+        constexpr int want = (PP % 32) / q * q;
+        return 6 * NPS + ((want - 6 * NPS) % 32 + 32) % 32;
+    }
     template <typename T>
     SESNT_HD static constexpr size_t stage_offset() { return ((sizeof(T) * SMEM_T + 127) / 128) * 128; }
     template <typename T>
     SESNT_HD static constexpr size_t smem(bool stage) {
-        return stage ? stage_offset<T>() + sizeof(T) * (size_t)G * 6 * NPS + 16 : sizeof(T) * SMEM_T;
+        return stage ? stage_offset<T>() + sizeof(T) * (size_t)G * stage_stride<T>() + 16 : sizeof(T) * SMEM_T;
     }
 };
 
@@ -55,10 +72,10 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols(const Step
     const long long units = (long long)a.nel * a.S;
     const long long ufirst = (long long)blockIdx.x * G;
     const int nunits = (int)(units - ufirst < G ? units - ufirst : G);  // units of this block
+    constexpr int SS = C::template stage_stride<T>();
     T *stage = reinterpret_cast<T *>(smem_raw + C::template stage_offset<T>());
-    uint64_t *mbar = reinterpret_cast<uint64_t *>(smem_raw + C::template stage_offset<T>() +
-                                                  sizeof(T) * (size_t)G * 6 * NPS);
-    const uint32_t stage_bytes = (uint32_t)(sizeof(T) * (size_t)nunits * 6 * NPS);  // a multiple of 16
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(smem_raw + C::template stage_offset<T>() + sizeof(T) * (size_t)G * SS);
+    constexpr uint32_t unit_bytes = (uint32_t)(sizeof(T) * 6 * NPS);  // a multiple of 16
     bool issued = false;
     if constexpr (STAGE) {
         if (t == 0) {
@@ -66,8 +83,9 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols(const Step
             tma_mbar_init(mb);
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
             if (!a.drop_completion && in_range((size_t)(ufirst + nunits) * 6 * NPS - 1, (size_t)units * 6 * NPS, a.err)) {
-                tma_expect(mb, stage_bytes);
-                tma_load_unit(stage, a.sig + (size_t)ufirst * 6 * NPS, stage_bytes, mb, a.piece);
+                tma_expect(mb, unit_bytes * (uint32_t)nunits);
+                for (int u = 0; u < nunits; ++u)
+                    tma_load_unit(stage + (size_t)u * SS, a.sig + (size_t)(ufirst + u) * 6 * NPS, unit_bytes, mb, a.piece);
                 issued = true;
             }
         }
@@ -76,7 +94,7 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols(const Step
     const int gl = t / PP;
     const int c = t - gl * PP;
     const int i = c % P, j = c / P;
-    T *sv = sD + 4 * PP + (size_t)gl * 9 * NP;  // this unit's [3][NP] velocity slab
+    T *sv = sD + 4 * PP + (size_t)gl * C::US;   // this unit's [3][NP] velocity slab
     T *sx = sv + 3 * NP;                        // [3][NP] x fluxes (xx, xy, xz weighted)
     T *sy = sx + 3 * NP;                        // [3][NP] y fluxes
     const long long unit = ufirst + gl;
@@ -97,7 +115,7 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols(const Step
     const size_t u0 = act ? unique_index<N>(a.NXU, a.NYU, ex, ey, ez, i, j, 0) : 0;
     const size_t l0 = (size_t)e * NP + c;        // element-local index of (i, j, 0)
     // this column's stress at k = 0: the staged copy or global memory
-    T *sig = STAGE ? stage + (size_t)gl * 6 * NPS + c : a.sig + (size_t)unit * 6 * NPS + c;
+    T *sig = STAGE ? stage + (size_t)gl * SS + c : a.sig + (size_t)unit * 6 * NPS + c;
     T vc[3][P];  // this column's velocity
     if (act) {
         const T *vs = a.v + (size_t)s * 3 * nuni;
@@ -227,7 +245,8 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols(const Step
     if constexpr (STAGE) {
         if (t == 0) {
             if (ok) {
-                tma_store(a.sig + (size_t)ufirst * 6 * NPS, tma_smem(stage), stage_bytes);
+                for (int u = 0; u < nunits; ++u)
+                    tma_store(a.sig + (size_t)(ufirst + u) * 6 * NPS, tma_smem(stage + (size_t)u * SS), unit_bytes);
                 tma_commit();
             } else {
                 atomicExch(a.err, 1);

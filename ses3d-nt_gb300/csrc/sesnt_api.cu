@@ -1862,11 +1862,12 @@ int sesnt_run(sesnt_t *h, int it0, int nsteps) {
 
 int sesnt_run_timed(sesnt_t *h, int it0, int nsteps, float *ms) {
     if (!h || !ms) return SESNT_EINVAL;
-    // prepare (uploads, graph) outside the timed region
+    Range r("sesnt_run_timed");
+    // prepare (uploads, graphs) outside the timed region
     int rc = h->dbl ? prepare_run<double>(h) : prepare_run<float>(h);
     if (rc) return rc;
-    if (h->use_graph && nsteps >= kGraphSteps && !h->graph) {
-        rc = h->dbl ? build_graph<double>(h) : build_graph<float>(h);
+    if (h->use_graph) {
+        rc = h->dbl ? prebuild_graphs<double>(h) : prebuild_graphs<float>(h);
         if (rc) return rc;
     }
     cudaEventRecord(h->ev0, h->stream);
@@ -1881,6 +1882,7 @@ int sesnt_run_timed(sesnt_t *h, int it0, int nsteps, float *ms) {
 
 int sesnt_run_profiled(sesnt_t *h, int it0, int nsteps, float ms[4]) {
     if (!h || !ms) return SESNT_EINVAL;
+    Range r("sesnt_run_profiled");
     for (int q = 0; q < 4; ++q) ms[q] = 0.0f;
     if (it0 < 1 || it0 + nsteps - 1 > h->g.nt)
         return h->fail(SESNT_ERANGE, "steps %d..%d outside 1..nt=%d", it0, it0 + nsteps - 1, h->g.nt);

@@ -74,7 +74,8 @@ extern "C" {
                                        elastic batches, else one point per thread */
 #define SESNT_ELEMENT_POINT 1       /* one thread per element-local point */
 #define SESNT_ELEMENT_PAIR 2        /* two simulations per thread (even elastic batches) */
-#define SESNT_ELEMENT_STAGE 3       /* SLS state staged by bulk copy, stored by bulk copy (degrees 4-7) */
+#define SESNT_ELEMENT_STAGE 3       /* SLS state staged by bulk copy, stored by bulk copy (degrees 4-7);
+                                       arg 1: one lane per warp waits for the copy (also for _STAGE_REG) */
 #define SESNT_ELEMENT_STAGE_REG 4   /* the same, stored from registers */
 #define SESNT_ELEMENT_PERSISTENT 5  /* persistent blocks fed by bulk copies */
 #define SESNT_ELEMENT_COLUMNS 6     /* one thread per (i, j) column of an element (elastic); arg
@@ -246,8 +247,10 @@ int sesnt_synchronize(sesnt_t *h);
 /* No counterpart in the reference. Tunes the element kernel on this handle's
  * grid, precision and batch: times every variant that computes this step
  * (one point per thread, paired simulations, one thread per column at four
- * register budgets with the stress loaded per point or staged per block, the staged kernel with bulk or register stores and
- * 0/4/8/16 KB copy pieces, the persistent kernel) with CUDA events on the
+ * register budgets with the stress loaded per point or staged per block,
+ * the staged kernel with bulk or register stores, 0/8/16 KB copy pieces and
+ * its wait polled by every thread or by one lane per warp, the persistent
+ * kernel) with CUDA events on the
  * handle's stream, keeps the fastest and appends it to the tuning cache
  * ($SESNT_TUNE_CACHE, else $HOME/.cache/sesnt-tune.txt), keyed by GPU name,
  * SM count, degree, precision, SLS, anisotropy, batch and grid. Runs the

@@ -65,6 +65,19 @@ __device__ __forceinline__ bool tma_try_wait(uint32_t mbar, uint32_t parity, int
     return done != 0;
 }
 
+// The same wait polled by lane 0 of each warp only: the outcome goes to the
+// other lanes by shuffle, and __syncwarp orders their later reads of the
+// landed data after lane 0's acquiring wait. Every thread of the warp must
+// call it. Where all lanes poll, each poll is a shared-memory operation per
+// lane.
+__device__ __forceinline__ bool tma_try_wait_warp(uint32_t mbar, uint32_t parity, int polls) {
+    bool done = false;
+    if ((threadIdx.x & 31) == 0) done = tma_try_wait(mbar, parity, polls);
+    done = __shfl_sync(0xffffffffu, done ? 1 : 0, 0) != 0;
+    __syncwarp();
+    return done;
+}
+
 // Bulk copies of one state unit are issued in pieces of at most `piece`
 // bytes (StepArgs::piece, a multiple of 16; 0: one copy per unit), so every
 // piece starts 16-byte aligned inside the 16-byte aligned unit. The 33 KB
@@ -327,7 +340,9 @@ __global__ void __launch_bounds__(StageCfg<N, T, NSLS>::NT, StageCfg<N, T, NSLS>
     __syncthreads();  // velocity slab, derivative tables and the mbarrier's initialisation
     T ev[9];
     if (act) strain_contract<N, T>(sD, sv, sv + NP, sv + 2 * NP, i, j, k, ev);
-    const bool landed = tma_try_wait(tma_smem(mbar), 0, a.wait_polls);
+    // variant_arg bit 0: lane 0 of each warp polls for the whole warp
+    const bool landed = (a.variant_arg & 1) ? tma_try_wait_warp(tma_smem(mbar), 0, a.wait_polls)
+                                            : tma_try_wait(tma_smem(mbar), 0, a.wait_polls);
     if (act && landed) {
         T sg[6], m[6][MS];
 #pragma unroll

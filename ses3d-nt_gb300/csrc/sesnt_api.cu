@@ -1450,7 +1450,8 @@ struct TuneChoice {
 // one point per thread; paired simulations (even elastic batches); one
 // thread per column at each instantiated resident-block count, with the
 // stress loaded per point or staged per block (elastic);
-// the staged kernel with bulk or register stores and four piece sizes (SLS);
+// the staged kernel with bulk or register stores, three piece sizes and the
+// stage's wait polled by every thread or by one lane per warp (SLS);
 // the persistent kernel.
 std::vector<TuneChoice> tune_candidates(const sesnt_t *h) {
     std::vector<TuneChoice> c = {{kVarPoint, 0, 8192}};
@@ -1460,7 +1461,8 @@ std::vector<TuneChoice> tune_candidates(const sesnt_t *h) {
         for (int m = 0; m < 4; ++m) c.push_back({kVarColumnsStaged, m, 0});
     } else {
         for (int v : {kVarStage, kVarStageReg})
-            for (int piece : {0, 4096, 8192, 16384}) c.push_back({v, 0, piece});
+            for (int piece : {0, 8192, 16384})
+                for (int arg : {0, 1}) c.push_back({v, arg, piece});
     }
     for (int piece : {0, 8192}) c.push_back({kVarPersistent, 0, piece});
     return c;

@@ -103,7 +103,8 @@ struct StepArgs {
     int stage;       // SLS steps: state staged in shared memory by bulk copy (k_element_stage)
     int contraction; // element kernel contractions: 0 CUDA cores, 1 tensor cores TF32x3, 2 tensor cores BF16x3
     int variant;     // ElementVariant
-    int variant_arg; // k_element_cols: index of the resident-block count (kColsMinb, 0..3)
+    int variant_arg; // k_element_cols: index of the resident-block count (kColsMinb, 0..3);
+                     // k_element_stage: bit 0 = one lane per warp polls the stage's mbarrier
     int piece;       // bulk copies of a state unit in pieces of this many bytes (multiple of 16; 0: whole)
     T two_over_d[3]; // 2/dx_elm, 2/dy_elm, 2/dz_elm
     int *err;        // device error word (a bounded wait ran out)

@@ -63,6 +63,41 @@ def test_column_kernel_matches_point_kernel(gpu, sesnt_lib, lpd, precision):
                 assert e < tol and ev < tol
 
 
+@pytest.mark.parametrize("lpd", [4, 5, 6, 7])
+def test_staged_kernel_wait_modes_agree(gpu, sesnt_lib, lpd):
+    """The staged SLS kernel with the stage's wait polled by every thread and
+    by one lane per warp, with bulk and register stores: the same step."""
+    for precision in (4, 8):
+        tol = 1e-5 if precision == 4 else 1e-12
+        wl = batch_of(with_grid(small_workload(lpd, n_sls=3, nt=100), precision=precision), 2)
+        base, vb, name_b, _, _ = run(wl, 100, sesnt.ELEMENT_STAGE, 0, 8192)
+        assert name_b == "k_element_stage"
+        for variant in (sesnt.ELEMENT_STAGE, sesnt.ELEMENT_STAGE_REG):
+            s, v, _, choice, _ = run(wl, 100, variant, 1, 0)
+            e, ev = rel_l2(s, base), rel_l2(v, vb)
+            print("lpd %d prec %d variant %d lane-0 wait: %.2e, vz %.2e" % (lpd, precision, variant, e, ev))
+            assert choice[:2] == (variant, 1) and e < tol and ev < tol
+
+
+def test_lane_zero_stage_wait_runs_out_and_reports(gpu, sesnt_lib):
+    """The one-lane-per-warp stage wait is bounded like the all-thread one."""
+    wl = small_workload(4, n_sls=3, nt=40)
+    with sesnt.Simulation(wl.grid) as sim:
+        workloads.setup(sim, wl)
+        sim.set_element_variant(sesnt.ELEMENT_STAGE, 1, 0)
+        sim.set_wait_limit(64, drop_completion=True)
+        sim.run(1, 2)
+        with pytest.raises(sesnt.SesntError) as e:
+            sim.synchronize()
+        assert e.value.code == sesnt.ETIMEOUT
+        sim.set_wait_limit(1 << 22)
+        sim.reset()
+        sim.run(1, 40)
+        again = sim.seismograms()
+    fresh, _, _, _, _ = run(wl, 40, sesnt.ELEMENT_POINT)
+    assert rel_l2(again, fresh) < 1e-5
+
+
 def test_staged_column_wait_runs_out_and_reports(gpu, sesnt_lib):
     """The staged column kernel's one mbarrier wait per block is bounded:
     with its bulk load dropped the wait runs out, synchronising returns

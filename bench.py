@@ -548,14 +548,16 @@ def run_served(args):
     and 1..n sources) arriving as a Poisson process, served concurrently by
     the request server, against the plain path (every source of every request
     run alone, one after another). Sizes are the served workload's ranges
-    scaled down (see `ranges`) so that the run ends in minutes."""
+    scaled down (see `ranges`, set by --lateral, --radial, --step-range and
+    --sources) so that the run ends in minutes."""
     import threading as _th
 
     import numpy as np
 
     import sesnt
     import workloads
-    ranges = dict(lateral=(16, 48), radial=(8, 24), lpds=(4, 6), steps=(300, 1500), sources=(1, 8), receivers=16)
+    ranges = dict(lateral=tuple(args.lateral), radial=tuple(args.radial), lpds=(4, 6), steps=tuple(args.step_range),
+                  sources=tuple(args.sources), receivers=16)
     stream = workloads.served_stream(args.requests, seed=5, **ranges)
     reqs = [workloads.request_of(w) for w in stream]
     hbm, peak_kind = peaks()
@@ -647,6 +649,10 @@ def main():
     ap.add_argument("--requests", type=int, default=40, help="served stream: number of requests")
     ap.add_argument("--rates", type=float, nargs="+", default=[2.0, 8.0], help="served stream: arrivals per second")
     ap.add_argument("--max-active", type=int, default=16, help="served stream: concurrent batches")
+    ap.add_argument("--lateral", type=int, nargs=2, default=[16, 48], help="served stream: lateral elements")
+    ap.add_argument("--radial", type=int, nargs=2, default=[8, 24], help="served stream: radial elements")
+    ap.add_argument("--step-range", type=int, nargs=2, default=[300, 1500], help="served stream: steps")
+    ap.add_argument("--sources", type=int, nargs=2, default=[1, 8], help="served stream: sources per request")
     ap.add_argument("--profile-steps", type=int, default=20)
     ap.add_argument("--accuracy-steps", type=int, default=1500)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)

@@ -456,9 +456,10 @@ def batched_headline(args):
 
 
 def accuracy(args, wl):
-    """FP32 (plain and Kahan-compensated velocity update) against the FP64
-    build of the same kernels: relative L2 of the seismograms of the first
-    simulation and of its final vz after accuracy_steps steps."""
+    """FP32 (plain, Kahan-compensated velocity update, force assembled in
+    FP64, tensor-core contractions) against the FP64 build of the same
+    kernels: relative L2 of the seismograms of the first simulation and of
+    its final vz after accuracy_steps steps."""
     import numpy as np
 
     import sesnt
@@ -466,6 +467,7 @@ def accuracy(args, wl):
     n = min(args.accuracy_steps, wl.grid.nt)
     res = {}
     for name, prec, flags in (("fp32", 4, 0), ("fp32_kahan", 4, sesnt.FLAG_KAHAN),
+                              ("fp32_force64", 4, sesnt.FLAG_FORCE64),
                               ("fp32_tc_tf32x3", 4, sesnt.FLAG_TC_TF32X3),
                               ("fp32_tc_bf16x3", 4, sesnt.FLAG_TC_BF16X3), ("fp64", 8, 0)):
         w = copy.copy(wl)
@@ -480,7 +482,7 @@ def accuracy(args, wl):
             res[name] = (sim.seismograms()[0].astype(np.float64), sim.field("vz", precision=8))
     rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
     out = {"steps": n}
-    for name in ("fp32", "fp32_kahan", "fp32_tc_tf32x3", "fp32_tc_bf16x3"):
+    for name in ("fp32", "fp32_kahan", "fp32_force64", "fp32_tc_tf32x3", "fp32_tc_bf16x3"):
         out[name] = {"seismogram_rel_l2": rel(res[name][0], res["fp64"][0]),
                      "vz_rel_l2": rel(res[name][1], res["fp64"][1])}
     return out

@@ -67,6 +67,9 @@ extern "C" {
                                      are available after the steps of a rotation snapshot) */
 #define SESNT_FLAG_AUTOTUNE 512u  /* sesnt_set_model applies the tuning cache's choice for this GPU
                                      and grid, or runs sesnt_tune and caches its choice */
+#define SESNT_FLAG_FORCE64 1024u  /* FP32 wavefields: assemble the force of shared points in FP64
+                                     (FP64 atomic adds, 12 more bytes per unique point and step);
+                                     FP64 handles already do */
 
 /* element-kernel variants (sesnt_set_element_variant); every variant computes
  * the same step, up to the order of the atomic adds */

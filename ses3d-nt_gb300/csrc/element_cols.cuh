@@ -220,7 +220,6 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols(const Step
             dti[q] = Dt[i * P + q];
             dtj[q] = Dt[j * P + q];
         }
-        T *F = a.F + (size_t)s * 3 * nuni;
 #pragma unroll
         for (int k = 0; k < P; ++k) {
             T fx = 0, fy = 0, fz = 0;
@@ -234,9 +233,7 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols(const Step
                 fz += zf[2][q] * dk + col[2 * NP + P * q] * dj + row[2 * NP + q] * di;
             }
             const size_t u = u0 + k * kstep;
-            atomicAdd(F + u, fx);
-            atomicAdd(F + nuni + u, fy);
-            atomicAdd(F + 2 * nuni + u, fz);
+            add_force(a, s, u, fx, fy, fz);
         }
     };
     // updated stress in the stage: visible to the bulk-copy engine after the barrier

@@ -290,10 +290,7 @@ __global__ void __launch_bounds__(TcCfg<N, PREC>::NT) k_element_tc(const StepArg
         const T fx = slab[0 * NP + p] + slab[3 * NP + p] + slab[6 * NP + p];
         const T fy = slab[1 * NP + p] + slab[4 * NP + p] + slab[7 * NP + p];
         const T fz = slab[2 * NP + p] + slab[5 * NP + p] + slab[8 * NP + p];
-        T *F = a.F + (size_t)s * 3 * nuni;
-        atomicAdd(F + u, fx);
-        atomicAdd(F + nuni + u, fy);
-        atomicAdd(F + 2 * nuni + u, fz);
+        add_force(a, s, u, fx, fy, fz);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();

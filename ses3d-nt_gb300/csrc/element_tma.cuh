@@ -236,10 +236,7 @@ __global__ void __launch_bounds__(TmaCfg<N, T, NSLS>::NT, TmaCfg<N, T, NSLS>::MI
         if (act) {
             T fx = 0, fy = 0, fz = 0;
             point_divergence<N, T>(sD + 3 * P * P, sf, i, j, k3, fx, fy, fz);
-            T *F = a.F + (size_t)s * 3 * nuni;
-            atomicAdd(F + u, fx);
-            atomicAdd(F + nuni + u, fy);
-            atomicAdd(F + 2 * nuni + u, fz);
+            add_force(a, s, u, fx, fy, fz);
         }
         __syncthreads();  // sv and sf are rewritten by the next unit
     }
@@ -372,10 +369,7 @@ __global__ void __launch_bounds__(StageCfg<N, T, NSLS>::NT, StageCfg<N, T, NSLS>
     if (ok && act) {
         T fx = 0, fy = 0, fz = 0;
         point_divergence<N, T>(sD + 3 * P * P, sf, i, j, k, fx, fy, fz);
-        T *F = a.F + (size_t)s * 3 * nuni;
-        atomicAdd(F + u, fx);
-        atomicAdd(F + nuni + u, fy);
-        atomicAdd(F + 2 * nuni + u, fz);
+        add_force(a, s, u, fx, fy, fz);
     }
     if (!ok && t == 0) {
         atomicExch(a.err, 1);

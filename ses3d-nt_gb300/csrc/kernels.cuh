@@ -96,6 +96,25 @@ __device__ __forceinline__ bool in_range(size_t idx, size_t n, int *err) {
 #endif
 }
 
+// Assembly of one element-local point's force into the unique-point force of
+// simulation s (replaces src/evolution.f90:372-388 and
+// src/communicate_fields.F90:48-247): FP32 atomic adds into F, or with
+// SESNT_FLAG_FORCE64 FP64 atomic adds into F64. The assembled force of a
+// smooth field is a small difference of large per-element contributions;
+// summed in FP64 it loses no digits to that cancellation.
+template <typename T>
+__device__ __forceinline__ void add_force(const StepArgs<T> &a, int s, size_t u, T fx, T fy, T fz) {
+    const size_t nuni = (size_t)a.nuni;
+    if (a.F64) {
+        double *F = a.F64 + (size_t)s * 3 * nuni;
+        atomicAdd(F + u, (double)fx);
+        atomicAdd(F + nuni + u, (double)fy);
+        atomicAdd(F + 2 * nuni + u, (double)fz);
+    } else {
+        add_force(a, s, u, fx, fy, fz);
+    }
+}
+
 // Evict-first hints: measured faster on the stores only (loads without the
 // hint keep the next blocks' shared velocity lines warm).
 #ifndef SESNT_HINT_LOADS
@@ -632,13 +651,8 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::M
             by += f1[5 * NP + pz_] * dk + f1[4 * NP + py_] * dj + f1[3 * NP + px_] * di;
             bz += f1[8 * NP + pz_] * dk + f1[7 * NP + py_] * dj + f1[6 * NP + px_] * di;
         }
-        T *F0 = a.F + (size_t)s0 * 3 * nuni, *F1 = F0 + 3 * nuni;
-        atomicAdd(F0 + u, ax);
-        atomicAdd(F0 + nuni + u, ay);
-        atomicAdd(F0 + 2 * nuni + u, az);
-        atomicAdd(F1 + u, bx);
-        atomicAdd(F1 + nuni + u, by);
-        atomicAdd(F1 + 2 * nuni + u, bz);
+        add_force(a, s0, u, ax, ay, az);
+        add_force(a, s0 + 1, u, bx, by, bz);
     }
 }
 
@@ -713,10 +727,7 @@ __global__ void __launch_bounds__(((ElemCfg<N>::NP + 31) / 32) * 32) k_sources(c
     const size_t nuni = (size_t)a.nuni;
     const size_t u =
         (size_t)(ex * N + i) + (size_t)a.NXU * ((size_t)(ey * N + j) + (size_t)a.NYU * (size_t)(ez * N + k));
-    T *F = a.F + (size_t)rec.sim * 3 * nuni;
-    atomicAdd(F + u, fx);
-    atomicAdd(F + nuni + u, fy);
-    atomicAdd(F + 2 * nuni + u, fz);
+    add_force(a, rec.sim, u, fx, fy, fz);
 }
 
 // Decode a unique point into the element-local copy with the lowest element
@@ -737,12 +748,15 @@ __global__ void __launch_bounds__(256) k_node(const StepArgs<T> a) {
     T *__restrict__ F = a.F + (size_t)s * 3 * nuni + u;
     T *__restrict__ v = a.v + (size_t)s * 3 * nuni + u;
     T *__restrict__ vc = KAHAN ? a.vc + (size_t)s * 3 * nuni + u : nullptr;
+    double *__restrict__ F64 = a.F64 ? a.F64 + (size_t)s * 3 * nuni + u : nullptr;
     // all loads before any store (stores to possibly aliasing arrays would
     // otherwise serialise each thread's later loads behind them)
     T f[3], vo[3], co[3] = {0, 0, 0};
+    double fd[3] = {0.0, 0.0, 0.0};
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        f[c] = F[c * nuni];
+        if (F64) fd[c] = F64[c * nuni];
+        else f[c] = F[c * nuni];
         vo[c] = v[c * nuni];
         if constexpr (KAHAN) co[c] = vc[c * nuni];
     }
@@ -756,8 +770,14 @@ __global__ void __launch_bounds__(256) k_node(const StepArgs<T> a) {
     const T tp = taper_value(a.px[ex * P + i], a.py[ey * P + j], a.pz[ez * P + k], a.inv_alpha);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        F[c * nuni] = T(0);
-        const T acc = f[c] * im;
+        T acc;
+        if (F64) {
+            F64[c * nuni] = 0.0;
+            acc = (T)(fd[c] * (double)im);  // the FP64 force rounded once, with the mass divide
+        } else {
+            F[c * nuni] = T(0);
+            acc = f[c] * im;
+        }
         if constexpr (KAHAN) {
             // Kahan-compensated v += dt*acc (the compensation is tapered with v)
             const T y = a.dt * acc - co[c];

@@ -298,6 +298,7 @@ struct sesnt_handle {
     double *dsin = nullptr, *dr = nullptr, *dw = nullptr;
     void *lam = nullptr, *mu = nullptr, *A = nullptr, *B = nullptr, *C = nullptr, *tau = nullptr;
     void *sig = nullptr, *mem = nullptr, *v = nullptr, *vc = nullptr, *F = nullptr, *invM = nullptr;
+    double *F64 = nullptr;  // SESNT_FLAG_FORCE64 on FP32 handles: the force accumulated in FP64
     int *d_it = nullptr;
     int *d_err = nullptr;  // set by a kernel whose bounded wait ran out
     int wait_polls = 1 << 22, drop_completion = 0;
@@ -487,6 +488,7 @@ struct sesnt_handle {
         a.lam = (const T *)lam; a.mu = (const T *)mu; a.A = (const T *)A; a.B = (const T *)B; a.C = (const T *)C;
         a.tau = (const T *)tau;
         a.sig = (T *)sig; a.mem = (T *)mem; a.v = (T *)v; a.vc = (T *)vc; a.F = (T *)F; a.invM = (const T *)invM;
+        a.F64 = F64;
         a.st_cs = state_cs(); a.st_unit = (long long)state_unit();
         a.nsrc = nsrc_rec; a.nt = g.nt; a.n_src_vm = n_src_vm; a.n_src_data = n_src_data; a.src = (const SrcRec *)d_src; a.src_vm = (const T *)d_src_vm;
         a.src_data = (const T *)d_src_data;
@@ -668,6 +670,7 @@ int zero_state(sesnt_t *h) {
         {h->v, E * 3 * (size_t)h->nuni * h->S},
         {h->vc, h->kahan ? E * 3 * (size_t)h->nuni * h->S : 0},
         {h->F, E * 3 * (size_t)h->nuni * h->S},
+        {h->F64, h->F64 ? 8 * 3 * (size_t)h->nuni * h->S : 0},
         {h->d_seis, E * (size_t)h->S * h->rec_elem.size() * 3 * h->g.nt},
         {h->d_xseis, E * (size_t)h->S * h->nxtr * h->g.nt},
         {h->du, E * 9 * (size_t)h->nloc * h->S},
@@ -1629,6 +1632,7 @@ size_t footprint(const sesnt_grid_t *g, bool aniso) {
     b += nloc * E * (2 + (aniso ? 3 : 0) + (g->n_sls ? 1 : 0));    // lambda, mu, A,B,C, tau
     b += nel * state_unit((int)NP, g->n_sls ? kNsls : 0) * E * S;  // sigma and memory variables (StateLayout)
     b += nuni * E * (1 + S * (6 + ((g->flags & SESNT_FLAG_KAHAN) ? 3 : 0)));  // invM, v, F, comp
+    if ((g->flags & SESNT_FLAG_FORCE64) && E == 4) b += nuni * 8 * 3 * S;     // FP64 force
     b += nloc * E * S * (((g->flags & SESNT_FLAG_STRAIN) ? 9 : 0) + ((g->flags & SESNT_FLAG_ROTATION) ? 6 : 0));
     b += nloc * (sizeof(float) + E);                                // set_model staging + rhoinv (transient)
     b += 1 << 20;                                                   // tables, counters
@@ -1721,6 +1725,11 @@ int sesnt_create(const sesnt_grid_t *grid, sesnt_t **out) {
             g_create_error = h->err;
             return rc;
         }
+    }
+    if ((grid->flags & SESNT_FLAG_FORCE64) && !h->dbl &&
+        (rc = h->alloc((void **)&h->F64, 3 * nuni * 8 * S, "FP64 force"))) {
+        g_create_error = h->err;
+        return rc;
     }
     if (h->kahan && (rc = h->alloc(&h->vc, 3 * nuni * E * S, "compensation"))) {
         g_create_error = h->err;

@@ -80,6 +80,7 @@ struct StepArgs {
     const T *lam, *mu, *A, *B, *C, *tau;
     // state
     T *sig, *mem, *v, *vc, *F;
+    double *F64;  // the force in FP64 (SESNT_FLAG_FORCE64 on FP32 handles), or null
     const T *invM;
     // sources
     int nsrc, nt;

@@ -35,6 +35,7 @@ FLAG_ROTATION = 64
 FLAG_NO_PAIR = 128
 FLAG_NO_STAGE = 256
 FLAG_AUTOTUNE = 512
+FLAG_FORCE64 = 1024
 (ELEMENT_AUTO, ELEMENT_POINT, ELEMENT_PAIR, ELEMENT_STAGE, ELEMENT_STAGE_REG, ELEMENT_PERSISTENT, ELEMENT_COLUMNS,
  ELEMENT_COLUMNS_STAGED) = range(8)
 SOURCE_MT, SOURCE_SF = 0, 1

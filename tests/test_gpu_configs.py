@@ -192,7 +192,8 @@ def test_config3_generator_lpd6_variants_match_oracle(gpu, sesnt_lib, oracle_mod
     assert e < 1e-6
     for k in names:
         assert rel_l2(f64[k], fo64[k]) < 1e-10, k
-    variants = (("FP32", 0, TOL), ("Kahan", sesnt.FLAG_KAHAN, TOL), ("TF32x3", sesnt.FLAG_TC_TF32X3, TOL),
+    variants = (("FP32", 0, TOL), ("Kahan", sesnt.FLAG_KAHAN, TOL), ("FP64 force", sesnt.FLAG_FORCE64, TOL),
+                ("TF32x3", sesnt.FLAG_TC_TF32X3, TOL),
                 ("BF16x3", sesnt.FLAG_TC_BF16X3, 1e-3))
     for label, flags, tol in variants:
         s, f = gpu(with_grid(wl, flags=flags).grid)

@@ -627,3 +627,32 @@ def test_checkpoint_and_resume(gpu, sesnt_lib, flags):
         with pytest.raises(sesnt.SesntError) as e:
             sim.load_state(ck)
         assert e.value.code == sesnt.EINVAL
+
+
+@pytest.mark.parametrize("lpd,n_sls,batch", [(4, 3, 1), (6, 3, 2), (4, 0, 4), (5, 0, 1)])
+def test_fp64_force_assembly(gpu, sesnt_lib, oracle_mod, lpd, n_sls, batch):
+    """SESNT_FLAG_FORCE64 (FP32 wavefields, force of shared points assembled
+    with FP64 atomics) computes the step of the FP32 oracle within 1e-4, in
+    every element kernel it can run with (staged, paired, point), and stays
+    at least as close to the FP64 build as plain FP32 (within 20%)."""
+    wl = small_workload(lpd, n_sls=n_sls, nt=300)
+    g = copy.copy(wl.grid)
+    g.batch = batch
+    srcs = []
+    for s in range(batch):
+        src = copy.copy(wl.sources[0])
+        src.sim, src.lat = s, 34.5 + 0.5 * s
+        srcs.append(src)
+    bw = workloads.Workload("f64force", g, wl.model, srcs, wl.receivers)
+    s32, _, _ = run_gpu(bw, 300, fields=())
+    s64f, _, _ = run_gpu(with_grid(bw, flags=sesnt.FLAG_FORCE64), 300, fields=())
+    s64, _, _ = run_gpu(with_grid(bw, precision=8), 300, fields=())
+    one = workloads.Workload("one", wl.grid, wl.model, [copy.copy(srcs[0])], wl.receivers)
+    one.sources[0].sim = 0
+    so, _, _ = run_oracle(oracle_mod, one, 300)
+    e_o = rel_l2(s64f[0], so)
+    e32, e64f = rel_l2(s32, s64), rel_l2(s64f, s64)
+    print("lpd %d n_sls %d batch %d: FP64-force vs oracle %.2e; vs FP64 build %.2e (plain FP32 %.2e)"
+          % (lpd, n_sls, batch, e_o, e64f, e32))
+    assert e_o < TOL
+    assert e64f < 1.2 * e32 + 1e-7

@@ -267,6 +267,8 @@ def run_ours(args):
     g = wl.grid
     g.flags |= {"persistent": sesnt.FLAG_PERSISTENT_ELEMENT, "tc_tf32x3": sesnt.FLAG_TC_TF32X3,
                 "tc_bf16x3": sesnt.FLAG_TC_BF16X3, "unstaged": sesnt.FLAG_NO_STAGE}.get(args.element, 0)
+    if args.force64:
+        g.flags |= sesnt.FLAG_FORCE64
     S = g.batch
     hbm, peak_kind = peaks()
 
@@ -306,6 +308,7 @@ def run_ours(args):
                    "l2": "inputs larger than L2 (%.2f GB touched per step vs 0.13 GB L2)"
                          % (info["algorithmic_bytes_per_step"] / 1e9),
                    "graph": not (g.flags & sesnt.FLAG_NO_GRAPH), "element": args.element,
+                   "force_assembly": "fp64" if args.force64 else "fp32",
                    "element_kernel": {"name": kname, "variant": choice[0], "arg": choice[1], "piece": choice[2],
                                       "tuning": tune_report.strip().splitlines()[1:] if tune_report else None},
                    "parallelism": "replicas" if WORLD > 1 else "single GPU"},
@@ -660,6 +663,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-seconds", type=float, default=60.0)
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
+    ap.add_argument("--force64", action="store_true",
+                    help="assemble the force in FP64 (SESNT_FLAG_FORCE64) in the measured run")
     ap.add_argument("--no-batched", dest="batched", action="store_false",
                     help="skip the batched-against-plain comparison of the default run")
     ap.add_argument("--element", default="tuned",

@@ -1092,8 +1092,10 @@ int launch_element(const StepArgs<T> &a, bool sls, bool aniso, void *stream) {
         case ElemKernel::StageReg:
             if constexpr (ElemCfg<N>::EPB == 1) {
                 const int store = k == ElemKernel::StageBulk ? 1 : 0;
-                const int r = aniso ? launch_element_stage<N, T, kNsls, true>(a, store, stream)
-                                    : launch_element_stage<N, T, kNsls, false>(a, store, stream);
+                // the wait mode (variant_arg) only where the staged kernel was chosen
+                if (a.variant != kVarStage && a.variant != kVarStageReg) b.variant_arg = 0;
+                const int r = aniso ? launch_element_stage<N, T, kNsls, true>(b, store, stream)
+                                    : launch_element_stage<N, T, kNsls, false>(b, store, stream);
                 return r > 0 ? -1 : r;
             }
             return -1;

@@ -111,7 +111,10 @@ __device__ __forceinline__ void add_force(const StepArgs<T> &a, int s, size_t u,
         atomicAdd(F + nuni + u, (double)fy);
         atomicAdd(F + 2 * nuni + u, (double)fz);
     } else {
-        add_force(a, s, u, fx, fy, fz);
+        T *F = a.F + (size_t)s * 3 * nuni;
+        atomicAdd(F + u, fx);
+        atomicAdd(F + nuni + u, fy);
+        atomicAdd(F + 2 * nuni + u, fz);
     }
 }
 
@@ -489,10 +492,7 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::M
     if (act) {
         T fx = 0, fy = 0, fz = 0;
         point_divergence<N, T>(sD + 3 * P * P, sf + le * 9 * NP, i, j, k, fx, fy, fz);
-        T *F = a.F + (size_t)s * 3 * nuni;
-        atomicAdd(F + u, fx);
-        atomicAdd(F + nuni + u, fy);
-        atomicAdd(F + 2 * nuni + u, fz);
+        add_force(a, s, u, fx, fy, fz);
     }
 }
 

@@ -78,6 +78,20 @@ __device__ __forceinline__ bool tma_try_wait_warp(uint32_t mbar, uint32_t parity
     return done;
 }
 
+// A hint that brings [p, p + bytes) of global memory into L2 (bulk
+// prefetch; no completion, no effect on results). The range is narrowed to
+// 16-byte boundaries inside [lo, hi), the buffer it belongs to.
+__device__ __forceinline__ void l2_prefetch(const void *p, size_t bytes, const void *lo, const void *hi) {
+    uintptr_t a = (uintptr_t)p, b = a + bytes;
+    const uintptr_t l = ((uintptr_t)lo + 15) & ~(uintptr_t)15, h = (uintptr_t)hi & ~(uintptr_t)15;
+    a = a < l ? l : (a & ~(uintptr_t)15);
+    b = b > h ? h : ((b + 15) & ~(uintptr_t)15);
+    for (; a < b; a += 16384) {  // in pieces of at most 16 KB
+        const uint32_t n = (uint32_t)(b - a < 16384 ? b - a : 16384);
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"(n) : "memory");
+    }
+}
+
 // Bulk copies of one state unit are issued in pieces of at most `piece`
 // bytes (StepArgs::piece, a multiple of 16; 0: one copy per unit), so every
 // piece starts 16-byte aligned inside the 16-byte aligned unit. The 33 KB
@@ -305,6 +319,18 @@ __global__ void __launch_bounds__(StageCfg<N, T, NSLS>::NT, StageCfg<N, T, NSLS>
             tma_expect(mb, C::STAGE_BYTES);
             tma_load_unit(st, a.sig + sb * C::UNIT, C::STAGE_BYTES, mb, a.piece);
             issued = true;
+        }
+        // L2 prefetch of the state and material of the unit a.prefetch ahead:
+        // about the unit the block that next takes this slot will load
+        const size_t units = (size_t)a.nel * S, ahead = sb + (size_t)a.prefetch;
+        if (a.prefetch > 0 && ahead < units) {
+            l2_prefetch(a.sig + ahead * C::UNIT, C::STAGE_BYTES, a.sig, a.sig + units * C::UNIT);
+            if (ahead % S == 0) {  // the material once per element
+                const size_t e2 = ahead / S, nl = (size_t)a.nel * NP;
+                l2_prefetch(a.lam + e2 * NP, NP * sizeof(T), a.lam, a.lam + nl);
+                l2_prefetch(a.mu + e2 * NP, NP * sizeof(T), a.mu, a.mu + nl);
+                if constexpr (NSLS > 0) l2_prefetch(a.tau + e2 * NP, NP * sizeof(T), a.tau, a.tau + nl);
+            }
         }
     }
     for (int x = t; x < 4 * P * P; x += NT) sD[x] = a.tabD[x];

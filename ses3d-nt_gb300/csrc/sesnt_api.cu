@@ -502,6 +502,10 @@ struct sesnt_handle {
         a.variant = variant;
         a.variant_arg = variant_arg;
         a.piece = piece;
+        {
+            static const int kWaveNum[4] = {0, 1, 2, 4};  // prefetch distance in halves of a wave
+            a.prefetch = kWaveNum[(variant_arg >> 1) & 3] * 8 * sms / 2;
+        }
         a.two_over_d[0] = (T)two_over_d[0];
         a.two_over_d[1] = (T)two_over_d[1];
         a.two_over_d[2] = (T)two_over_d[2];
@@ -1453,8 +1457,9 @@ struct TuneChoice {
 // one point per thread; paired simulations (even elastic batches); one
 // thread per column at each instantiated resident-block count, with the
 // stress loaded per point or staged per block (elastic);
-// the staged kernel with bulk or register stores, three piece sizes and the
-// stage's wait polled by every thread or by one lane per warp (SLS);
+// the staged kernel with bulk or register stores, two piece sizes, the
+// stage's wait polled by every thread or by one lane per warp, and an L2
+// prefetch of the state half a wave, one or two waves ahead (SLS);
 // the persistent kernel.
 std::vector<TuneChoice> tune_candidates(const sesnt_t *h) {
     std::vector<TuneChoice> c = {{kVarPoint, 0, 8192}};
@@ -1464,8 +1469,8 @@ std::vector<TuneChoice> tune_candidates(const sesnt_t *h) {
         for (int m = 0; m < 4; ++m) c.push_back({kVarColumnsStaged, m, 0});
     } else {
         for (int v : {kVarStage, kVarStageReg})
-            for (int piece : {0, 8192, 16384})
-                for (int arg : {0, 1}) c.push_back({v, arg, piece});
+            for (int piece : {0, 8192})
+                for (int arg : {0, 1, 2, 4, 6}) c.push_back({v, arg, piece});
     }
     for (int piece : {0, 8192}) c.push_back({kVarPersistent, 0, piece});
     return c;
@@ -2104,7 +2109,9 @@ int sesnt_tune(sesnt_t *h, char *report, int report_len) {
 int sesnt_set_element_variant(sesnt_t *h, int variant, int arg, int piece) {
     if (!h) return SESNT_EINVAL;
     if (variant < kVarAuto || variant >= kVarCount) return h->fail(SESNT_EINVAL, "unknown element variant %d", variant);
-    if (arg < 0 || arg > 3) return h->fail(SESNT_EINVAL, "variant argument %d outside 0..3", arg);
+    if (arg < 0 || arg > 7) return h->fail(SESNT_EINVAL, "variant argument %d outside 0..7", arg);
+    if ((variant == kVarColumns || variant == kVarColumnsStaged) && arg > 3)
+        return h->fail(SESNT_EINVAL, "column-kernel argument %d outside 0..3", arg);
     if (piece < 0 || piece % 16 != 0) return h->fail(SESNT_EINVAL, "piece size %d is not a multiple of 16 bytes", piece);
     h->drop_graph();  // the graphs hold the launch arguments
     h->variant = variant;

@@ -52,6 +52,8 @@ cases = [  # lpd, n_sls, aniso, kind, flags, batch[, (variant, arg, piece) or "t
     (4, 3, False, sesnt.SOURCE_MT, 0, 1, "tune", 8),
     (4, 3, False, sesnt.SOURCE_MT, sesnt.FLAG_FORCE64, 2),
     (4, 0, False, sesnt.SOURCE_SF, sesnt.FLAG_FORCE64, 4, (C, 1, 0)),
+    (4, 3, True, sesnt.SOURCE_MT, 0, 3, (sesnt.ELEMENT_STAGE, 7, 0)),
+    (6, 3, False, sesnt.SOURCE_MT, 0, 1, (SR, 6, 8192), 8),
 ]
 for case in cases:
     lpd, n_sls, aniso, kind, flags, batch = case[:6]
@@ -102,4 +104,4 @@ def test_every_kernel_in_bounds(gpu, tmp_path):
     code = SCRIPT % (PKG, HERE, str(tmp_path))
     r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=900)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
-    assert "OK 22" in r.stdout
+    assert "OK 24" in r.stdout

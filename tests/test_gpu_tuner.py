@@ -65,18 +65,20 @@ def test_column_kernel_matches_point_kernel(gpu, sesnt_lib, lpd, precision):
 
 @pytest.mark.parametrize("lpd", [4, 5, 6, 7])
 def test_staged_kernel_wait_modes_agree(gpu, sesnt_lib, lpd):
-    """The staged SLS kernel with the stage's wait polled by every thread and
-    by one lane per warp, with bulk and register stores: the same step."""
+    """The staged SLS kernel with the stage's wait polled by every thread or
+    by one lane per warp, with and without the L2 prefetch of the state
+    ahead, with bulk and register stores: the same step."""
     for precision in (4, 8):
         tol = 1e-5 if precision == 4 else 1e-12
         wl = batch_of(with_grid(small_workload(lpd, n_sls=3, nt=100), precision=precision), 2)
         base, vb, name_b, _, _ = run(wl, 100, sesnt.ELEMENT_STAGE, 0, 8192)
         assert name_b == "k_element_stage"
         for variant in (sesnt.ELEMENT_STAGE, sesnt.ELEMENT_STAGE_REG):
-            s, v, _, choice, _ = run(wl, 100, variant, 1, 0)
-            e, ev = rel_l2(s, base), rel_l2(v, vb)
-            print("lpd %d prec %d variant %d lane-0 wait: %.2e, vz %.2e" % (lpd, precision, variant, e, ev))
-            assert choice[:2] == (variant, 1) and e < tol and ev < tol
+            for arg in (1, 2, 4, 7):
+                s, v, _, choice, _ = run(wl, 100, variant, arg, 0)
+                e, ev = rel_l2(s, base), rel_l2(v, vb)
+                print("lpd %d prec %d variant %d arg %d: %.2e, vz %.2e" % (lpd, precision, variant, arg, e, ev))
+                assert choice[:2] == (variant, arg) and e < tol and ev < tol
 
 
 def test_lane_zero_stage_wait_runs_out_and_reports(gpu, sesnt_lib):

@@ -79,7 +79,7 @@ extern "C" {
 #define SESNT_ELEMENT_PAIR 2        /* two simulations per thread (even elastic batches) */
 #define SESNT_ELEMENT_STAGE 3       /* SLS state staged by bulk copy, stored by bulk copy (degrees 4-7);
                                        arg bit 0: one lane per warp waits for the copy; bits 1-2: L2
-                                       prefetch of the state 1/2, 1 or 2 resident waves ahead (both
+                                       prefetch of the state 1/4, 1/2 or 1 resident wave ahead (both
                                        also for _STAGE_REG) */
 #define SESNT_ELEMENT_STAGE_REG 4   /* the same, stored from registers */
 #define SESNT_ELEMENT_PERSISTENT 5  /* persistent blocks fed by bulk copies */
@@ -255,7 +255,8 @@ int sesnt_synchronize(sesnt_t *h);
  * register budgets with the stress loaded per point or staged per block,
  * the staged kernel with bulk or register stores, 0/8 KB copy pieces, its
  * wait polled by every thread or by one lane per warp and an L2 prefetch of
- * the state ahead of it, the persistent kernel) with CUDA events on the
+ * the state 1/4, 1/2 or 1 wave of resident blocks ahead, the persistent
+ * kernel) with CUDA events on the
  * handle's stream, keeps the fastest and appends it to the tuning cache
  * ($SESNT_TUNE_CACHE, else $HOME/.cache/sesnt-tune.txt), keyed by GPU name,
  * SM count, degree, precision, SLS, anisotropy, batch and grid. Runs the

@@ -503,8 +503,9 @@ struct sesnt_handle {
         a.variant_arg = variant_arg;
         a.piece = piece;
         {
-            static const int kWaveNum[4] = {0, 1, 2, 4};  // prefetch distance in halves of a wave
-            a.prefetch = kWaveNum[(variant_arg >> 1) & 3] * 8 * sms / 2;
+            // L2 prefetch distance: 0, 1/4, 1/2 or 1 wave of 8 resident blocks per SM
+            static const int kQuarters[4] = {0, 1, 2, 4};
+            a.prefetch = kQuarters[(variant_arg >> 1) & 3] * 8 * sms / 4;
         }
         a.two_over_d[0] = (T)two_over_d[0];
         a.two_over_d[1] = (T)two_over_d[1];
@@ -1457,9 +1458,10 @@ struct TuneChoice {
 // one point per thread; paired simulations (even elastic batches); one
 // thread per column at each instantiated resident-block count, with the
 // stress loaded per point or staged per block (elastic);
-// the staged kernel with bulk or register stores, two piece sizes, the
-// stage's wait polled by every thread or by one lane per warp, and an L2
-// prefetch of the state half a wave, one or two waves ahead (SLS);
+// the staged kernel with bulk or register stores, one copy per unit or 8 KB
+// pieces, the stage's wait polled by every thread or by one lane per warp,
+// and an L2 prefetch of the state a quarter, half or whole wave of resident
+// blocks ahead (SLS);
 // the persistent kernel.
 std::vector<TuneChoice> tune_candidates(const sesnt_t *h) {
     std::vector<TuneChoice> c = {{kVarPoint, 0, 8192}};
@@ -1468,9 +1470,10 @@ std::vector<TuneChoice> tune_candidates(const sesnt_t *h) {
         for (int m = 0; m < 4; ++m) c.push_back({kVarColumns, m, 8192});
         for (int m = 0; m < 4; ++m) c.push_back({kVarColumnsStaged, m, 0});
     } else {
-        for (int v : {kVarStage, kVarStageReg})
-            for (int piece : {0, 8192})
-                for (int arg : {0, 1, 2, 4, 6}) c.push_back({v, arg, piece});
+        for (int v : {kVarStage, kVarStageReg}) {
+            for (int arg : {0, 1, 2, 4, 6}) c.push_back({v, arg, 0});
+            c.push_back({v, 0, 8192});
+        }
     }
     for (int piece : {0, 8192}) c.push_back({kVarPersistent, 0, piece});
     return c;

@@ -106,8 +106,8 @@ struct StepArgs {
     int variant;     // ElementVariant
     int variant_arg; // k_element_cols: index of the resident-block count (kColsMinb, 0..3);
                      // k_element_stage: bit 0 = one lane per warp polls the stage's mbarrier,
-                     // bits 1-2 = L2 prefetch distance in resident waves (0: none, 1: 1/2,
-                     // 2: 1, 3: 2 waves of 8 blocks per SM)
+                     // bits 1-2 = L2 prefetch distance in resident waves (0: none, 1: 1/4,
+                     // 2: 1/2, 3: 1 wave of 8 blocks per SM)
     int piece;       // bulk copies of a state unit in pieces of this many bytes (multiple of 16; 0: whole)
     int prefetch;    // k_element_stage: L2 prefetch of the unit this many units ahead (0: none)
     T two_over_d[3]; // 2/dx_elm, 2/dy_elm, 2/dz_elm

@@ -84,8 +84,9 @@ extern "C" {
 #define SESNT_ELEMENT_STAGE_REG 4   /* the same, stored from registers */
 #define SESNT_ELEMENT_PERSISTENT 5  /* persistent blocks fed by bulk copies */
 #define SESNT_ELEMENT_COLUMNS 6     /* one thread per (i, j) column of an element (elastic); arg
-                                       selects the resident blocks per SM the kernel is sized for
-                                       (0: 4, 1: 5, 2: 6, 3: 8) */
+                                       bits 0-1 select the resident blocks per SM the kernel is sized
+                                       for (0: 4, 1: 5, 2: 6, 3: 8), bits 2-3 an L2 prefetch of the
+                                       stress 1/4, 1/2 or 1 resident wave ahead */
 #define SESNT_ELEMENT_COLUMNS_STAGED 7 /* the same with each block's stress staged by bulk copy */
 
 /* source kinds (sesnt_add_source) */

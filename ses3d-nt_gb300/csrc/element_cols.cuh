@@ -90,6 +90,22 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols(const Step
             }
         }
     }
+    if (t == 0 && a.prefetch > 0 && ufirst + a.prefetch < units) {
+        // L2 prefetch of the stress and material of the units a.prefetch
+        // ahead: about those the block that next takes this slot will load
+        const long long u1 = ufirst + a.prefetch, u2 = u1 + G < units ? u1 + G : units;
+        l2_prefetch(a.sig + (size_t)u1 * 6 * NPS, sizeof(T) * (size_t)(u2 - u1) * 6 * NPS, a.sig,
+                    a.sig + (size_t)units * 6 * NPS);
+        const size_t e1 = (size_t)(u1 / a.S), e2 = (size_t)((u2 - 1) / a.S) + 1, nl = (size_t)a.nel * NP;
+        const size_t bytes = sizeof(T) * (e2 - e1) * NP;
+        l2_prefetch(a.lam + e1 * NP, bytes, a.lam, a.lam + nl);
+        l2_prefetch(a.mu + e1 * NP, bytes, a.mu, a.mu + nl);
+        if constexpr (ANISO) {
+            l2_prefetch(a.A + e1 * NP, bytes, a.A, a.A + nl);
+            l2_prefetch(a.B + e1 * NP, bytes, a.B, a.B + nl);
+            l2_prefetch(a.C + e1 * NP, bytes, a.C, a.C + nl);
+        }
+    }
     for (int x = t; x < 4 * PP; x += NT) sD[x] = a.tabD[x];
     const int gl = t / PP;
     const int c = t - gl * PP;

@@ -1100,13 +1100,13 @@ int launch_element(const StepArgs<T> &a, bool sls, bool aniso, void *stream) {
             }
             return -1;
         case ElemKernel::Columns: {
-            const int r = aniso ? launch_element_cols<N, T, true, false>(a, a.variant_arg, stream)
-                                : launch_element_cols<N, T, false, false>(a, a.variant_arg, stream);
+            const int r = aniso ? launch_element_cols<N, T, true, false>(a, a.variant_arg & 3, stream)
+                                : launch_element_cols<N, T, false, false>(a, a.variant_arg & 3, stream);
             return r > 0 ? -1 : r;
         }
         case ElemKernel::ColumnsStaged: {
-            const int r = aniso ? launch_element_cols<N, T, true, true>(a, a.variant_arg, stream)
-                                : launch_element_cols<N, T, false, true>(a, a.variant_arg, stream);
+            const int r = aniso ? launch_element_cols<N, T, true, true>(a, a.variant_arg & 3, stream)
+                                : launch_element_cols<N, T, false, true>(a, a.variant_arg & 3, stream);
             return r > 0 ? -1 : r;
         }
         case ElemKernel::Pair: b.pair = 1; break;

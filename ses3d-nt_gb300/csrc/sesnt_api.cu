@@ -268,6 +268,10 @@ struct HostSource {
 
 }  // namespace
 
+// Resident-block budgets of the column kernel (kColsMinb in element_cols.cuh),
+// for the host's prefetch distances.
+constexpr int kColsMinbHost[4] = {4, 5, 6, 8};
+
 struct sesnt_handle {
     sesnt_grid_t g{};
     int N = 0, P = 0, NP = 0, nel = 0, S = 1;
@@ -503,9 +507,17 @@ struct sesnt_handle {
         a.variant_arg = variant_arg;
         a.piece = piece;
         {
-            // L2 prefetch distance: 0, 1/4, 1/2 or 1 wave of 8 resident blocks per SM
+            // L2 prefetch distance: 0, 1/4, 1/2 or 1 wave of resident blocks, in
+            // (element, simulation) units: the staged kernel has 8 blocks of one
+            // unit per SM; the column kernels the budget of arg bits 0-1 with
+            // G units per block
             static const int kQuarters[4] = {0, 1, 2, 4};
-            a.prefetch = kQuarters[(variant_arg >> 1) & 3] * 8 * sms / 4;
+            if (variant == kVarColumns || variant == kVarColumnsStaged) {
+                const int pp = (N + 1) * (N + 1), gpb = pp <= 128 ? 128 / pp : 1;
+                a.prefetch = kQuarters[(variant_arg >> 2) & 3] * kColsMinbHost[variant_arg & 3] * gpb * sms / 4;
+            } else {
+                a.prefetch = kQuarters[(variant_arg >> 1) & 3] * 8 * sms / 4;
+            }
         }
         a.two_over_d[0] = (T)two_over_d[0];
         a.two_over_d[1] = (T)two_over_d[1];
@@ -1467,8 +1479,10 @@ std::vector<TuneChoice> tune_candidates(const sesnt_t *h) {
     std::vector<TuneChoice> c = {{kVarPoint, 0, 8192}};
     if (!h->sls) {
         if (h->S % 2 == 0) c.push_back({kVarPair, 0, 8192});
-        for (int m = 0; m < 4; ++m) c.push_back({kVarColumns, m, 8192});
-        for (int m = 0; m < 4; ++m) c.push_back({kVarColumnsStaged, m, 0});
+        for (int m = 0; m < 3; ++m)
+            for (int q = 0; q < 4; ++q) c.push_back({kVarColumns, m | (q << 2), 8192});
+        c.push_back({kVarColumns, 3, 8192});
+        for (int m = 0; m < 2; ++m) c.push_back({kVarColumnsStaged, m, 0});
     } else {
         for (int v : {kVarStage, kVarStageReg}) {
             for (int arg : {0, 1, 2, 4, 6}) c.push_back({v, arg, 0});
@@ -2112,9 +2126,9 @@ int sesnt_tune(sesnt_t *h, char *report, int report_len) {
 int sesnt_set_element_variant(sesnt_t *h, int variant, int arg, int piece) {
     if (!h) return SESNT_EINVAL;
     if (variant < kVarAuto || variant >= kVarCount) return h->fail(SESNT_EINVAL, "unknown element variant %d", variant);
-    if (arg < 0 || arg > 7) return h->fail(SESNT_EINVAL, "variant argument %d outside 0..7", arg);
-    if ((variant == kVarColumns || variant == kVarColumnsStaged) && arg > 3)
-        return h->fail(SESNT_EINVAL, "column-kernel argument %d outside 0..3", arg);
+    if (arg < 0 || arg > 15) return h->fail(SESNT_EINVAL, "variant argument %d outside 0..15", arg);
+    if ((variant == kVarStage || variant == kVarStageReg) && arg > 7)
+        return h->fail(SESNT_EINVAL, "staged-kernel argument %d outside 0..7", arg);
     if (piece < 0 || piece % 16 != 0) return h->fail(SESNT_EINVAL, "piece size %d is not a multiple of 16 bytes", piece);
     h->drop_graph();  // the graphs hold the launch arguments
     h->variant = variant;

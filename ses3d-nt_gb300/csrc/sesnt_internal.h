@@ -104,7 +104,8 @@ struct StepArgs {
     int stage;       // SLS steps: state staged in shared memory by bulk copy (k_element_stage)
     int contraction; // element kernel contractions: 0 CUDA cores, 1 tensor cores TF32x3, 2 tensor cores BF16x3
     int variant;     // ElementVariant
-    int variant_arg; // k_element_cols: index of the resident-block count (kColsMinb, 0..3);
+    int variant_arg; // k_element_cols: bits 0-1 index of the resident-block count (kColsMinb),
+                     // bits 2-3 L2 prefetch distance (0: none, 1: 1/4, 2: 1/2, 3: 1 wave);
                      // k_element_stage: bit 0 = one lane per warp polls the stage's mbarrier,
                      // bits 1-2 = L2 prefetch distance in resident waves (0: none, 1: 1/4,
                      // 2: 1/2, 3: 1 wave of 8 blocks per SM)

@@ -42,10 +42,10 @@ cases = [  # lpd, n_sls, aniso, kind, flags, batch[, (variant, arg, piece) or "t
     (5, 3, True, sesnt.SOURCE_SF, 0, 2),
     (6, 3, False, sesnt.SOURCE_MT, 0, 2),
     (7, 3, False, sesnt.SOURCE_MT, sesnt.FLAG_KAHAN, 1),
-    (2, 0, False, sesnt.SOURCE_MT, 0, 5, (C, 0, 0)),
+    (2, 0, False, sesnt.SOURCE_MT, 0, 5, (C, 12, 0)),
     (4, 0, True, sesnt.SOURCE_SF, 0, 3, (C, 1, 0)),
-    (4, 0, False, sesnt.SOURCE_MT, 0, 6, (CS, 1, 4096)),
-    (7, 0, True, sesnt.SOURCE_MT, 0, 3, (CS, 3, 0)),
+    (4, 0, False, sesnt.SOURCE_MT, 0, 6, (CS, 9, 4096)),
+    (7, 0, True, sesnt.SOURCE_MT, 0, 3, (CS, 15, 0)),
     (6, 0, False, sesnt.SOURCE_MT, 0, 2, (C, 0, 0), 8),
     (5, 3, False, sesnt.SOURCE_MT, 0, 2, (SR, 0, 4096)),
     (4, 0, False, sesnt.SOURCE_MT, 0, 4, "tune"),

@@ -53,7 +53,7 @@ def test_column_kernel_matches_point_kernel(gpu, sesnt_lib, lpd, precision):
         assert name_p == "k_element"
         for variant, kname in ((sesnt.ELEMENT_COLUMNS, "k_element_cols"),
                                (sesnt.ELEMENT_COLUMNS_STAGED, "k_element_cols (staged stress)")):
-            for arg in ((0, 1, 2, 3) if precision == 4 else (0,)):
+            for arg in ((0, 1, 2, 3, 5, 10, 15) if precision == 4 else (0, 6)):
                 sc, vcol, name_c, choice, _ = run(wl, 120, variant, arg, piece=0 if arg % 2 else 4096)
                 assert name_c == kname and choice[:2] == (variant, arg)
                 e, ev = rel_l2(sc, sp), rel_l2(vcol, vp)
@@ -189,7 +189,8 @@ def test_tuning_after_stepping_and_bad_variants_are_refused(gpu, sesnt_lib, tmp_
         assert ex.value.code == sesnt.ESTATE
         sim.reset()
         sim.tune()  # after a reset the wavefield is zero again
-        for bad in ((99, 0, 0), (sesnt.ELEMENT_COLUMNS, 7, 0), (sesnt.ELEMENT_STAGE, 0, 100)):
+        for bad in ((99, 0, 0), (sesnt.ELEMENT_COLUMNS, 16, 0), (sesnt.ELEMENT_STAGE, 8, 0),
+                    (sesnt.ELEMENT_STAGE, 0, 100)):
             with pytest.raises(sesnt.SesntError) as ex:
                 sim.set_element_variant(*bad)
             assert ex.value.code == sesnt.EINVAL

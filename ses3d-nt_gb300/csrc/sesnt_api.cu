@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <filesystem>
 #include <fstream>
 #include <limits>
 #include <sstream>
@@ -1539,6 +1540,9 @@ bool tune_cache_lookup(const std::string &key, TuneChoice *out) {
 void tune_cache_store(const std::string &key, const TuneChoice &c, double ms) {
     const std::string path = tune_cache_path();
     if (path.empty()) return;
+    std::error_code ec;  // the cache's directory (e.g. $HOME/.cache) may not exist yet
+    const std::filesystem::path dir = std::filesystem::path(path).parent_path();
+    if (!dir.empty()) std::filesystem::create_directories(dir, ec);
     std::ofstream f(path, std::ios::app);
     if (f) f << key << ' ' << c.variant << ' ' << c.arg << ' ' << c.piece << ' ' << ms << '\n';
 }
@@ -1552,6 +1556,19 @@ void tune_cache_store(const std::string &key, const TuneChoice &c, double ms) {
 template <typename T>
 int tune_impl(sesnt_t *h, TuneChoice *best_out, double *best_ms) {
     const LpdOps<T> *o = ops<T>(h);
+    // the handle's choice before tuning, restored if tuning fails
+    struct Keep {
+        sesnt_t *h;
+        int variant, arg, piece;
+        bool done = false;
+        ~Keep() {
+            if (!done) {
+                h->variant = variant;
+                h->variant_arg = arg;
+                h->piece = piece;
+            }
+        }
+    } keep{h, h->variant, h->variant_arg, h->piece};
     std::ostringstream rep;
     rep << "tuning " << tune_key(h) << "\n";
     TuneChoice best{kVarAuto, h->variant_arg, h->piece};
@@ -1573,29 +1590,24 @@ int tune_impl(sesnt_t *h, TuneChoice *best_out, double *best_ms) {
                                 (c.variant == kVarColumns && name == "k_element_cols") ||
                                 (c.variant == kVarColumnsStaged && name == "k_element_cols (staged stress)");
         if (!applicable) continue;
-        auto launch = [&](int n) {
+        // n launches between two events on the handle's stream; milliseconds, or < 0 on an error
+        auto timed = [&](int n) -> float {
+            float ms = -1.0f;
+            if (cudaEventRecord(h->ev0, h->stream) != cudaSuccess) return -1.0f;
             for (int q = 0; q < n; ++q)
-                if (o->element(a, h->sls, h->aniso, h->stream)) return false;
-            return true;
+                if (o->element(a, h->sls, h->aniso, h->stream)) return -1.0f;
+            if (cudaEventRecord(h->ev1, h->stream) != cudaSuccess || cudaEventSynchronize(h->ev1) != cudaSuccess ||
+                cudaEventElapsedTime(&ms, h->ev0, h->ev1) != cudaSuccess)
+                return -1.0f;
+            return ms;
         };
-        if (!launch(2)) return h->fail(SESNT_ECUDA, "tuning launch failed: %s", cudaGetErrorString(cudaGetLastError()));
-        float ms1 = 0.0f;
-        cudaEventRecord(h->ev0, h->stream);
-        launch(1);
-        cudaEventRecord(h->ev1, h->stream);
-        cudaError_t e = cudaEventSynchronize(h->ev1);
-        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms1, h->ev0, h->ev1);
-        if (e != cudaSuccess) return h->cuda_fail(e, "tuning");
+        const float ms1 = timed(2) >= 0.0f ? timed(1) : -1.0f;  // two warm launches, then one timed
+        if (ms1 < 0.0f) return h->fail(SESNT_ECUDA, "tuning launch failed: %s", cudaGetErrorString(cudaGetLastError()));
         const int n = std::max(3, std::min(200, (int)(2.0 / std::max(ms1, 1e-3f))));
         double t = 1e30;
         for (int rep_i = 0; rep_i < 3; ++rep_i) {
-            float ms = 0.0f;
-            cudaEventRecord(h->ev0, h->stream);
-            if (!launch(n)) return h->fail(SESNT_ECUDA, "tuning launch failed");
-            cudaEventRecord(h->ev1, h->stream);
-            e = cudaEventSynchronize(h->ev1);
-            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, h->ev0, h->ev1);
-            if (e != cudaSuccess) return h->cuda_fail(e, "tuning");
+            const float ms = timed(n);
+            if (ms < 0.0f) return h->fail(SESNT_ECUDA, "tuning launch failed: %s", cudaGetErrorString(cudaGetLastError()));
             t = std::min(t, (double)ms / n);
         }
         char line[256];
@@ -1612,6 +1624,7 @@ int tune_impl(sesnt_t *h, TuneChoice *best_out, double *best_ms) {
     h->variant = best.variant;
     h->variant_arg = best.arg;
     h->piece = best.piece;
+    keep.done = true;
     char line[160];
     std::snprintf(line, sizeof line, "chosen: variant %d arg %d piece %d (%.4f ms per element launch)\n", best.variant,
                   best.arg, best.piece, best_t);

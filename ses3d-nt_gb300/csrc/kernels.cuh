@@ -1046,8 +1046,9 @@ constexpr bool has_columns(bool stage) {
 // A variant chosen by the tuner or the caller (StepArgs::variant) where the
 // configuration has it; otherwise the rules: tensor-core contractions when
 // asked for; the persistent kernel when asked for; the staged kernel for SLS
-// steps of degrees 4-7; one point per thread, with paired simulations for
-// even elastic batches. The displacement gradient (du) is kept only by
+// steps of degrees 4-7 (at degree 4 in FP32 with the L2 prefetch half a
+// resident wave ahead, StepArgs::prefetch); one point per thread, with paired
+// simulations for even elastic batches. The displacement gradient (du) is kept only by
 // k_element.
 template <int N, typename T>
 ElemKernel plan_element(const StepArgs<T> &a, bool sls, bool aniso) {

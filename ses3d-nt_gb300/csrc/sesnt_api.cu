@@ -516,6 +516,10 @@ struct sesnt_handle {
             if (variant == kVarColumns || variant == kVarColumnsStaged) {
                 const int pp = (N + 1) * (N + 1), gpb = pp <= 128 ? 128 / pp : 1;
                 a.prefetch = kQuarters[(variant_arg >> 2) & 3] * kColsMinbHost[variant_arg & 3] * gpb * sms / 4;
+            } else if (variant == kVarAuto) {
+                // the launch rules' staged kernel prefetches half a wave ahead at degree 4 in
+                // FP32 (config 2: 0.2552 -> 0.2422 ms per element launch); at degree 6 it is slower
+                a.prefetch = (sls && N == 4 && !dbl) ? 2 * 8 * sms / 4 : 0;
             } else {
                 a.prefetch = kQuarters[(variant_arg >> 1) & 3] * 8 * sms / 4;
             }

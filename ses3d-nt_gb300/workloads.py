@@ -260,11 +260,15 @@ def config4(nt=3000, seed=4, batch=64, precision=4, nx=64, ny=64, nz=32):
 
 
 def setup(sim, wl):
-    """Load a workload into a sesnt.Simulation: model, sources, receivers.
-    Returns the receiver element indices (for reference)."""
-    from sesnt import locate_point, source_signature
+    """Load a workload into a sesnt.Simulation: model, sources, receivers."""
     m = wl.model
     sim.set_model(m["rhoinv"], m["lambda"], m["mu"], m.get("a"), m.get("b"), m.get("c"), m.get("q"))
+    setup_sources_receivers(sim, wl)
+
+
+def setup_sources_receivers(sim, wl):
+    """The sources and receivers of a workload, located and registered."""
+    from sesnt import locate_point, source_signature
     g = wl.grid
     for s in wl.sources:
         elem, vm = locate_point(g, s.lat, s.lon, s.depth)

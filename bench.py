@@ -358,15 +358,16 @@ def run_ours(args):
 def choose_element(sim, element):
     """Apply an --element choice that is not a grid flag: `tuned` runs the
     library's tuner on this grid (sesnt_tune, which also caches the choice
-    for SESNT_FLAG_AUTOTUNE handles), `columns` forces the column kernel.
+    for SESNT_FLAG_AUTOTUNE handles), `columns*` force a column kernel.
     Returns the tuning report or None."""
     import sesnt
     if element == "tuned":
         return sim.tune()
     if element.startswith("columns"):
-        arg = int(element.split(":")[1]) if ":" in element else 0
-        v = sesnt.ELEMENT_COLUMNS_STAGED if element.startswith("columns_staged") else sesnt.ELEMENT_COLUMNS
-        sim.set_element_variant(v, arg, 0)
+        kind, _, arg = element.partition(":")
+        v = {"columns": sesnt.ELEMENT_COLUMNS, "columns_staged": sesnt.ELEMENT_COLUMNS_STAGED,
+             "columns_pair": sesnt.ELEMENT_COLUMNS_PAIR}[kind]
+        sim.set_element_variant(v, int(arg or 0), 0)
     return None
 
 
@@ -677,7 +678,8 @@ def main():
                     help="skip the batched-against-plain comparison of the default run")
     ap.add_argument("--element", default="tuned",
                     choices=["tuned", "simple", "persistent", "unstaged", "tc_tf32x3", "tc_bf16x3"] +
-                            ["columns:%d" % q for q in range(4)] + ["columns_staged:%d" % q for q in range(4)],
+                            ["columns:%d" % q for q in range(4)] + ["columns_staged:%d" % q for q in range(4)] +
+                            ["columns_pair:%d" % q for q in (0, 1, 2, 3, 8, 9, 10)],
                     help="element kernel variant (all compute the full step): tuned = the library's tuner "
                          "picks on this grid; simple = the launch rules; tc_*: tcgen05 contractions")
     args = ap.parse_args()

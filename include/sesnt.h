@@ -88,6 +88,10 @@ extern "C" {
                                        for (0: 4, 1: 5, 2: 6, 3: 8), bits 2-3 an L2 prefetch of the
                                        stress 1/4, 1/2 or 1 resident wave ahead */
 #define SESNT_ELEMENT_COLUMNS_STAGED 7 /* the same with each block's stress staged by bulk copy */
+#define SESNT_ELEMENT_COLUMNS_PAIR 8 /* one thread per column and pair of simulations (even elastic
+                                        batches); arg bits 0-1 select the resident blocks per SM
+                                        (0: 4, 1: 3, 2 and 3: 2), bits 2-3 the L2 prefetch as for
+                                        _COLUMNS */
 
 /* source kinds (sesnt_add_source) */
 #define SESNT_SOURCE_MT 0 /* moment tensor: comp = Mxx Mxy Mxz Myy Myz Mzz */

@@ -52,6 +52,13 @@ struct ColCfg {
     SESNT_HD static constexpr size_t smem(bool stage) {
         return stage ? stage_offset<T>() + sizeof(T) * (size_t)G * stage_stride<T>() + 16 : sizeof(T) * SMEM_T;
     }
+    // k_element_cols2: slabs of (simulation 0, simulation 1) value pairs,
+    // one unit every US2 pairs, congruent to PP modulo 16 so that thread t
+    // finds the pair c of its unit in banks 2t and 2t + 1 (mod 32) for 4-byte
+    // values (4t .. 4t + 3 for 8-byte values), as US does for single values.
+    static constexpr int US2 = 9 * NP + ((PP - 9 * NP) % 16 + 16) % 16;
+    template <typename T>
+    SESNT_HD static constexpr size_t smem2() { return sizeof(T) * (4 * PP + 2 * (size_t)G * US2); }
 };
 
 // STAGE: thread 0 bulk-copies the block's stress range (G units of 6 x NPS
@@ -275,6 +282,291 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols(const Step
 }
 
 
+template <typename T>
+struct Vec2;
+template <>
+struct Vec2<float> {
+    using type = float2;
+};
+template <>
+struct Vec2<double> {
+    using type = double2;
+};
+
+// Two simulations per column thread (k_element_cols2), for even elastic
+// batches. A unit is an element and a pair of consecutive simulations
+// (2p, 2p + 1), whose stress units are adjacent in the element-major state.
+// The slabs hold (simulation 2p, simulation 2p + 1) value pairs, so one
+// 8-byte shared load (16 bytes in FP64) feeds both simulations' line
+// contractions, and the point's derivative-table registers, metric, taper,
+// material and index arithmetic serve both, as in k_element_pair. Each
+// thread keeps both simulations' column velocities and z fluxes in
+// registers. Per point and simulation the arithmetic and its order are
+// those of k_element_pair.
+template <int N, typename T, bool ANISO, int MINB>
+__global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols2(const StepArgs<T> a) {
+    using C = ColCfg<N>;
+    using V = typename Vec2<T>::type;
+    constexpr int P = C::P, PP = C::PP, NP = C::NP, G = C::G, NT = C::NT, NPS = C::NPS, US = C::US2;
+    extern __shared__ __align__(128) unsigned char cols_smem_raw[];
+    T *sD = reinterpret_cast<T *>(cols_smem_raw);  // [4][P*P]: Dx Dy Dz (scaled) | Dt
+    V *slab = reinterpret_cast<V *>(sD + 4 * PP);  // 16-byte aligned: 4 * PP values of T
+    const int t = threadIdx.x;
+    const int S2 = a.S / 2;
+    const long long units = (long long)a.nel * S2;
+    const long long ufirst = (long long)blockIdx.x * G;
+    const size_t ustate = (size_t)6 * NPS;                 // values of one simulation's stress unit
+    const size_t nstate = (size_t)a.nel * a.S * ustate;    // the whole stress array
+    if (t == 0 && a.prefetch > 0 && ufirst + a.prefetch < units) {
+        // L2 prefetch of the stress and material of the units a.prefetch ahead
+        const long long u1 = ufirst + a.prefetch, u2 = u1 + G < units ? u1 + G : units;
+        l2_prefetch(a.sig + (size_t)(2 * u1) * ustate, sizeof(T) * (size_t)(2 * (u2 - u1)) * ustate, a.sig,
+                    a.sig + nstate);
+        const size_t e1 = (size_t)(u1 / S2), e2 = (size_t)((u2 - 1) / S2) + 1, nl = (size_t)a.nel * NP;
+        const size_t bytes = sizeof(T) * (e2 - e1) * NP;
+        l2_prefetch(a.lam + e1 * NP, bytes, a.lam, a.lam + nl);
+        l2_prefetch(a.mu + e1 * NP, bytes, a.mu, a.mu + nl);
+        if constexpr (ANISO) {
+            l2_prefetch(a.A + e1 * NP, bytes, a.A, a.A + nl);
+            l2_prefetch(a.B + e1 * NP, bytes, a.B, a.B + nl);
+            l2_prefetch(a.C + e1 * NP, bytes, a.C, a.C + nl);
+        }
+    }
+    for (int x = t; x < 4 * PP; x += NT) sD[x] = a.tabD[x];
+    const int gl = t / PP;
+    const int c = t - gl * PP;
+    const int i = c % P, j = c / P;
+    V *sv = slab + (size_t)gl * US;  // this unit's [3][NP] velocity pairs
+    V *sx = sv + 3 * NP;             // [3][NP] x fluxes (xx, xy, xz weighted)
+    V *sy = sx + 3 * NP;             // [3][NP] y fluxes (xy, yy, yz weighted)
+    const long long unit = ufirst + gl;
+    const size_t nuni = (size_t)a.nuni, nloc = (size_t)a.nloc;
+    int e = 0, s0 = 0, ex = 0, ey = 0, ez = 0;
+    bool act = gl < G && unit < units;
+    if (act) {
+        e = (int)(unit / S2);
+        s0 = 2 * (int)(unit - (long long)e * S2);
+        ex = e % a.nx;
+        ey = (e / a.nx) % a.ny;
+        ez = e / (a.nx * a.ny);
+        act = in_range(unique_index<N>(a.NXU, a.NYU, ex, ey, ez, i, j, N), nuni, a.err) &&
+              in_range((size_t)e * NP + c + (size_t)PP * N, nloc, a.err) &&
+              in_range((size_t)(s0 + 1), (size_t)a.S, a.err) &&
+              in_range((size_t)(2 * unit + 1) * ustate + 5 * NPS + c + (size_t)PP * N, nstate, a.err);
+    }
+    const size_t kstep = (size_t)a.NXU * a.NYU;  // unique-index stride of k
+    const size_t u0 = act ? unique_index<N>(a.NXU, a.NYU, ex, ey, ez, i, j, 0) : 0;
+    const size_t l0 = (size_t)e * NP + c;        // element-local index of (i, j, 0)
+    const size_t soff = act ? (size_t)(2 * unit) * ustate + c : 0;
+    T *sig0 = a.sig + soff, *sig1 = sig0 + ustate;  // this column's stress at k = 0
+    T vc[2][3][P];  // the column's velocity, both simulations
+    if (act) {
+        const T *va = a.v + (size_t)s0 * 3 * nuni, *vb = va + 3 * nuni;
+#pragma unroll
+        for (int k = 0; k < P; ++k) {
+            const size_t u = u0 + k * kstep;
+            vc[0][0][k] = va[u];
+            vc[0][1][k] = va[nuni + u];
+            vc[0][2][k] = va[2 * nuni + u];
+            vc[1][0][k] = vb[u];
+            vc[1][1][k] = vb[nuni + u];
+            vc[1][2][k] = vb[2 * nuni + u];
+        }
+#pragma unroll
+        for (int k = 0; k < P; ++k) {
+#pragma unroll
+            for (int q = 0; q < 3; ++q) sv[q * NP + c + PP * k] = V{vc[0][q][k], vc[1][q][k]};
+        }
+    }
+    // material and stress of point k = 0, in flight across the barrier
+    T lam = 0, mu = 0, cA = 0, cB = 0, cC = 0, sg[2][6] = {{0, 0, 0, 0, 0, 0}, {0, 0, 0, 0, 0, 0}};
+    auto load_point = [&](int k, T &l, T &m_, T &A, T &B, T &Cc, T (&sgk)[2][6]) {
+        const size_t li = l0 + (size_t)PP * k;
+        l = ld_stream(a.lam + li);
+        m_ = ld_stream(a.mu + li);
+        if constexpr (ANISO) {
+            A = ld_stream(a.A + li);
+            B = ld_stream(a.B + li);
+            Cc = ld_stream(a.C + li);
+        }
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            sgk[0][q] = ld_stream(sig0 + q * NPS + PP * k);
+            sgk[1][q] = ld_stream(sig1 + q * NPS + PP * k);
+        }
+    };
+    if (act) load_point(0, lam, mu, cA, cB, cC, sg);
+    __syncthreads();  // tables and velocity slabs
+    const T *Dx = sD, *Dy = sD + PP, *Dz = sD + 2 * PP, *Dt = sD + 3 * PP;
+    T dxi[P], dyj[P];
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+        dxi[q] = Dx[q * P + i];
+        dyj[q] = Dy[q * P + j];
+    }
+    T zf[2][3][P];  // z fluxes of the column (xz, yz, zz weighted), both simulations
+    const T m0[6][1] = {{0}, {0}, {0}, {0}, {0}, {0}};
+#pragma unroll
+    for (int k = 0; k < P; ++k) {
+        T nlam = 0, nmu = 0, nA = 0, nB = 0, nC = 0, nsg[2][6] = {{0, 0, 0, 0, 0, 0}, {0, 0, 0, 0, 0, 0}};
+        if (k + 1 < P && act) load_point(k + 1, nlam, nmu, nA, nB, nC, nsg);
+        if (act) {
+            T e0[9], e1[9];
+#pragma unroll
+            for (int x = 0; x < 9; ++x) e0[x] = e1[x] = 0;
+            const V *row = sv + P * (j + P * k);  // x line (q, j, k)
+            const V *col = sv + i + PP * k;       // y line (i, q, k)
+#pragma unroll
+            for (int q = 0; q < P; ++q) {
+                const T dx = dxi[q], dy = dyj[q], dz = Dz[q * P + k];
+                const V rx = row[q], ry = row[NP + q], rz = row[2 * NP + q];
+                const V cx = col[P * q], cy = col[NP + P * q], cz = col[2 * NP + P * q];
+                e0[0] += rx.x * dx;
+                e0[1] += ry.x * dx;
+                e0[2] += rz.x * dx;
+                e0[3] += cx.x * dy;
+                e0[4] += cy.x * dy;
+                e0[5] += cz.x * dy;
+                e0[6] += vc[0][0][q] * dz;
+                e0[7] += vc[0][1][q] * dz;
+                e0[8] += vc[0][2][q] * dz;
+                e1[0] += rx.y * dx;
+                e1[1] += ry.y * dx;
+                e1[2] += rz.y * dx;
+                e1[3] += cx.y * dy;
+                e1[4] += cy.y * dy;
+                e1[5] += cz.y * dy;
+                e1[6] += vc[1][0][q] * dz;
+                e1[7] += vc[1][1][q] * dz;
+                e1[8] += vc[1][2][q] * dz;
+            }
+            T g0[9], g1[9];
+            complete_gradient<N, T>(a, e0, vc[0][0][k], vc[0][1][k], vc[0][2][k], i, k, ex, ez, g0);
+            complete_gradient<N, T>(a, e1, vc[1][0][k], vc[1][1][k], vc[1][2][k], i, k, ex, ez, g1);
+            const T tp = taper_value(a.px[ex * P + i], a.py[ey * P + j], a.pz[ez * P + k], a.inv_alpha);
+            const T rr = a.r[ez * P + k];
+            const T rs = rr * a.sin_t[ex * P + i];
+            const T W = a.w[i] * a.w[j] * a.w[k];
+            const T gx = W * rs * a.c1, gy = W * rr * a.c2, gz = W * (rr * rs) * a.c3;
+            T sn[2][6];  // integrated stress before the taper: xx xy xz yy yz zz
+            auto update = [&](const T(&gg)[9], const T(&sgv)[6], T *sig, T(&o)[6]) {
+                const T exx = gg[kDuXX], eyy = gg[kDuYY], ezz = gg[kDuZZ];
+                const T exy = (gg[kDuXY] + gg[kDuYX]) * T(0.5);
+                const T exz = (gg[kDuXZ] + gg[kDuZX]) * T(0.5);
+                const T eyz = (gg[kDuYZ] + gg[kDuZY]) * T(0.5);
+                T rxx, ryy, rzz, rxy, rxz, ryz;
+                stress_rates<T, 0, ANISO>(exx, eyy, ezz, exy, exz, eyz, lam, mu, T(0), cA, cB, cC, m0, rxx, ryy,
+                                          rzz, rxy, rxz, ryz);
+                o[0] = sgv[0] + a.dt * rxx;
+                o[1] = sgv[1] + a.dt * rxy;
+                o[2] = sgv[2] + a.dt * rxz;
+                o[3] = sgv[3] + a.dt * ryy;
+                o[4] = sgv[4] + a.dt * ryz;
+                o[5] = sgv[5] + a.dt * rzz;
+#pragma unroll
+                for (int q = 0; q < 6; ++q) st_stream(sig + q * NPS, o[q] * tp);
+            };
+            update(g0, sg[0], sig0 + PP * k, sn[0]);
+            update(g1, sg[1], sig1 + PP * k, sn[1]);
+            const int p = c + PP * k;
+            sx[p] = V{sn[0][0] * gx, sn[1][0] * gx};
+            sx[NP + p] = V{sn[0][1] * gx, sn[1][1] * gx};
+            sx[2 * NP + p] = V{sn[0][2] * gx, sn[1][2] * gx};
+            sy[p] = V{sn[0][1] * gy, sn[1][1] * gy};
+            sy[NP + p] = V{sn[0][3] * gy, sn[1][3] * gy};
+            sy[2 * NP + p] = V{sn[0][4] * gy, sn[1][4] * gy};
+#pragma unroll
+            for (int s = 0; s < 2; ++s) {
+                zf[s][0][k] = sn[s][2] * gz;
+                zf[s][1][k] = sn[s][4] * gz;
+                zf[s][2][k] = sn[s][5] * gz;
+            }
+        }
+        lam = nlam;
+        mu = nmu;
+        cA = nA;
+        cB = nB;
+        cC = nC;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            sg[0][q] = nsg[0][q];
+            sg[1][q] = nsg[1][q];
+        }
+    }
+    __syncthreads();  // x and y flux slabs
+    if (!act) return;
+    // weak divergence of the column's points, both simulations, and their assembly
+    T dti[P], dtj[P];
+#pragma unroll
+    for (int q = 0; q < P; ++q) {
+        dti[q] = Dt[i * P + q];
+        dtj[q] = Dt[j * P + q];
+    }
+#pragma unroll
+    for (int k = 0; k < P; ++k) {
+        T f[2][3] = {{0, 0, 0}, {0, 0, 0}};
+        const V *row = sx + P * (j + P * k);
+        const V *col = sy + i + PP * k;
+#pragma unroll
+        for (int q = 0; q < P; ++q) {
+            const T di = dti[q], dj = dtj[q], dk = Dt[k * P + q];
+            const V r0 = row[q], r1 = row[NP + q], r2 = row[2 * NP + q];
+            const V c0 = col[P * q], c1 = col[NP + P * q], c2 = col[2 * NP + P * q];
+            f[0][0] += zf[0][0][q] * dk + c0.x * dj + r0.x * di;
+            f[0][1] += zf[0][1][q] * dk + c1.x * dj + r1.x * di;
+            f[0][2] += zf[0][2][q] * dk + c2.x * dj + r2.x * di;
+            f[1][0] += zf[1][0][q] * dk + c0.y * dj + r0.y * di;
+            f[1][1] += zf[1][1][q] * dk + c1.y * dj + r1.y * di;
+            f[1][2] += zf[1][2][q] * dk + c2.y * dj + r2.y * di;
+        }
+        const size_t u = u0 + k * kstep;
+        add_force(a, s0, u, f[0][0], f[0][1], f[0][2]);
+        add_force(a, s0 + 1, u, f[1][0], f[1][1], f[1][2]);
+    }
+}
+
+// Resident blocks per SM the paired column kernel is sized for (FP32; FP64
+// uses 1). At degree 4 its 45 KB of slabs allow at most 4 blocks per SM; at
+// 2 blocks (175 registers in FP32) the kernel needs no cap on registers.
+constexpr int kCols2Minb[] = {4, 3, 2, 2};
+
+template <int N, typename T, bool ANISO, int MINB>
+int launch_element_cols2_m(const StepArgs<T> &a, void *stream) {
+    using C = ColCfg<N>;
+    if (a.S < 2 || a.S % 2 != 0) return 1;
+    const long long units = (long long)a.nel * (a.S / 2);
+    const size_t smem = C::template smem2<T>();
+    if (smem > kMaxSmemPerBlock) return 1;
+    k_element_cols2<N, T, ANISO, MINB><<<(unsigned)((units + C::G - 1) / C::G), C::NT, smem, (cudaStream_t)stream>>>(a);
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
+}
+
+// minb_idx selects kCols2Minb[] (FP32); returns 1 if this configuration has
+// no paired column kernel (the caller falls back).
+template <int N, typename T, bool ANISO>
+int launch_element_cols2(const StepArgs<T> &a, int minb_idx, void *stream) {
+    if constexpr (sizeof(T) == 8) {
+        return launch_element_cols2_m<N, T, ANISO, 1>(a, stream);
+    } else {
+        switch (minb_idx) {
+            case 0: return launch_element_cols2_m<N, T, ANISO, kCols2Minb[0]>(a, stream);
+            case 1: return launch_element_cols2_m<N, T, ANISO, kCols2Minb[1]>(a, stream);
+            case 2: return launch_element_cols2_m<N, T, ANISO, kCols2Minb[2]>(a, stream);
+            default: return launch_element_cols2_m<N, T, ANISO, kCols2Minb[3]>(a, stream);
+        }
+    }
+}
+
+template <int N, typename T, bool ANISO, int MINB>
+int prepare_element_cols2_m() {
+    const size_t smem = ColCfg<N>::template smem2<T>();
+    if (smem <= 48 * 1024 || smem > kMaxSmemPerBlock) return 0;
+    return cudaFuncSetAttribute(k_element_cols2<N, T, ANISO, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)smem) == cudaSuccess
+               ? 0
+               : -1;
+}
+
 // Resident blocks per SM the column kernel is sized for (FP32); FP64 uses 1
 // (as k_element). Selected per grid by the tuner among the instantiated
 // values.
@@ -320,10 +612,15 @@ int prepare_element_cols_m() {
 
 template <int N, typename T, bool ANISO>
 int prepare_element_cols() {
-    if constexpr (sizeof(T) == 8) return prepare_element_cols_m<N, T, ANISO, 1>();
+    if constexpr (sizeof(T) == 8)
+        return prepare_element_cols_m<N, T, ANISO, 1>() || prepare_element_cols2_m<N, T, ANISO, 1>() ? -1 : 0;
     else
         return prepare_element_cols_m<N, T, ANISO, kColsMinb[0]>() || prepare_element_cols_m<N, T, ANISO, kColsMinb[1]>() ||
-                       prepare_element_cols_m<N, T, ANISO, kColsMinb[2]>() || prepare_element_cols_m<N, T, ANISO, kColsMinb[3]>()
+                       prepare_element_cols_m<N, T, ANISO, kColsMinb[2]>() || prepare_element_cols_m<N, T, ANISO, kColsMinb[3]>() ||
+                       prepare_element_cols2_m<N, T, ANISO, kCols2Minb[0]>() ||
+                       prepare_element_cols2_m<N, T, ANISO, kCols2Minb[1]>() ||
+                       prepare_element_cols2_m<N, T, ANISO, kCols2Minb[2]>() ||
+                       prepare_element_cols2_m<N, T, ANISO, kCols2Minb[3]>()
                    ? -1
                    : 0;
 }

@@ -1005,7 +1005,7 @@ int launch_element_bulk(const StepArgs<T> &a, bool sls, bool aniso, void *stream
 // The element kernel one step launches, decided on the host from the
 // handle's configuration (plan_element) so that the launcher, the tuner and
 // the kernel name a caller reads agree.
-enum class ElemKernel : int { Tc, Point, Pair, StageBulk, StageReg, Persistent, Columns, ColumnsStaged };
+enum class ElemKernel : int { Tc, Point, Pair, StageBulk, StageReg, Persistent, Columns, ColumnsStaged, ColumnsPair };
 
 inline const char *elem_kernel_name(ElemKernel k) {
     switch (k) {
@@ -1017,6 +1017,7 @@ inline const char *elem_kernel_name(ElemKernel k) {
         case ElemKernel::Persistent: return "k_element_tma";
         case ElemKernel::Columns: return "k_element_cols";
         case ElemKernel::ColumnsStaged: return "k_element_cols (staged stress)";
+        case ElemKernel::ColumnsPair: return "k_element_cols2";
     }
     return "?";
 }
@@ -1043,6 +1044,11 @@ constexpr bool has_columns(bool stage) {
     return ColCfg<N>::template smem<T>(stage) <= kMaxSmemPerBlock;
 }
 
+template <int N, typename T>
+constexpr bool has_columns2() {
+    return ColCfg<N>::template smem2<T>() <= kMaxSmemPerBlock;
+}
+
 // A variant chosen by the tuner or the caller (StepArgs::variant) where the
 // configuration has it; otherwise the rules: tensor-core contractions when
 // asked for; the persistent kernel when asked for; the staged kernel for SLS
@@ -1063,6 +1069,7 @@ ElemKernel plan_element(const StepArgs<T> &a, bool sls, bool aniso) {
         case kVarPersistent: if (has_persistent<N, T>(sls, aniso)) return ElemKernel::Persistent; break;
         case kVarColumns: if (!sls && has_columns<N, T>(false)) return ElemKernel::Columns; break;
         case kVarColumnsStaged: if (!sls && has_columns<N, T>(true)) return ElemKernel::ColumnsStaged; break;
+        case kVarColumnsPair: if (!sls && even && has_columns2<N, T>()) return ElemKernel::ColumnsPair; break;
         default: break;
     }
     if (a.persistent && has_persistent<N, T>(sls, aniso)) return ElemKernel::Persistent;
@@ -1108,6 +1115,11 @@ int launch_element(const StepArgs<T> &a, bool sls, bool aniso, void *stream) {
         case ElemKernel::ColumnsStaged: {
             const int r = aniso ? launch_element_cols<N, T, true, true>(a, a.variant_arg & 3, stream)
                                 : launch_element_cols<N, T, false, true>(a, a.variant_arg & 3, stream);
+            return r > 0 ? -1 : r;
+        }
+        case ElemKernel::ColumnsPair: {
+            const int r = aniso ? launch_element_cols2<N, T, true>(a, a.variant_arg & 3, stream)
+                                : launch_element_cols2<N, T, false>(a, a.variant_arg & 3, stream);
             return r > 0 ? -1 : r;
         }
         case ElemKernel::Pair: b.pair = 1; break;

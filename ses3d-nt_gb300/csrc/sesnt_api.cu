@@ -301,9 +301,10 @@ cudaMemPool_t library_pool(int device) {
     return pools[device];
 }
 
-// Resident-block budgets of the column kernel (kColsMinb in element_cols.cuh),
-// for the host's prefetch distances.
+// Resident-block budgets of the column kernels (kColsMinb and kCols2Minb in
+// element_cols.cuh), for the host's prefetch distances.
 constexpr int kColsMinbHost[4] = {4, 5, 6, 8};
+constexpr int kCols2MinbHost[4] = {4, 3, 2, 2};
 
 struct sesnt_handle {
     sesnt_grid_t g{};
@@ -560,13 +561,15 @@ struct sesnt_handle {
         a.piece = piece;
         {
             // L2 prefetch distance: 0, 1/4, 1/2 or 1 wave of resident blocks, in
-            // (element, simulation) units: the staged kernel has 8 blocks of one
-            // unit per SM; the column kernels the budget of arg bits 0-1 with
-            // G units per block
+            // units of the kernel: the staged kernel has 8 blocks of one
+            // (element, simulation) unit per SM; the column kernels the budget
+            // of arg bits 0-1 with G units per block ((element, simulation
+            // pair) units for k_element_cols2)
             static const int kQuarters[4] = {0, 1, 2, 4};
-            if (variant == kVarColumns || variant == kVarColumnsStaged) {
+            if (variant == kVarColumns || variant == kVarColumnsStaged || variant == kVarColumnsPair) {
                 const int pp = (N + 1) * (N + 1), gpb = pp <= 128 ? 128 / pp : 1;
-                a.prefetch = kQuarters[(variant_arg >> 2) & 3] * kColsMinbHost[variant_arg & 3] * gpb * sms / 4;
+                const int minb = dbl ? 1 : (variant == kVarColumnsPair ? kCols2MinbHost : kColsMinbHost)[variant_arg & 3];
+                a.prefetch = kQuarters[(variant_arg >> 2) & 3] * minb * gpb * sms / 4;
             } else if (variant == kVarAuto) {
                 // the launch rules' staged kernel prefetches half a wave ahead at degree 4 in
                 // FP32 (config 2: 0.2552 -> 0.2422 ms per element launch); at degree 6 it is slower
@@ -1529,7 +1532,8 @@ struct TuneChoice {
 // (tensor-core contractions change the arithmetic and are never chosen):
 // one point per thread; paired simulations (even elastic batches); one
 // thread per column at each instantiated resident-block count, with the
-// stress loaded per point or staged per block (elastic);
+// stress loaded per point or staged per block, and with two simulations per
+// column thread (elastic);
 // the staged kernel with bulk or register stores, one copy per unit or 8 KB
 // pieces, the stage's wait polled by every thread or by one lane per warp,
 // and an L2 prefetch of the state a quarter, half or whole wave of resident
@@ -1543,6 +1547,9 @@ std::vector<TuneChoice> tune_candidates(const sesnt_t *h) {
             for (int q = 0; q < 4; ++q) c.push_back({kVarColumns, m | (q << 2), 8192});
         c.push_back({kVarColumns, 3, 8192});
         for (int m = 0; m < 2; ++m) c.push_back({kVarColumnsStaged, m, 0});
+        if (h->S % 2 == 0)
+            for (int m = 0; m < 3; ++m)
+                for (int q : {0, 2}) c.push_back({kVarColumnsPair, m | (q << 2), 8192});
     } else {
         for (int v : {kVarStage, kVarStageReg}) {
             for (int arg : {0, 1, 2, 4, 6}) c.push_back({v, arg, 0});
@@ -1647,7 +1654,8 @@ int tune_impl(sesnt_t *h, TuneChoice *best_out, double *best_ms) {
                                 (c.variant == kVarStageReg && name == "k_element_stage (register stores)") ||
                                 (c.variant == kVarPersistent && name == "k_element_tma") ||
                                 (c.variant == kVarColumns && name == "k_element_cols") ||
-                                (c.variant == kVarColumnsStaged && name == "k_element_cols (staged stress)");
+                                (c.variant == kVarColumnsStaged && name == "k_element_cols (staged stress)") ||
+                                (c.variant == kVarColumnsPair && name == "k_element_cols2");
         if (!applicable) continue;
         // n launches between two events on the handle's stream; milliseconds, or < 0 on an error
         auto timed = [&](int n) -> float {

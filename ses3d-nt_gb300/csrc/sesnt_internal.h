@@ -60,6 +60,7 @@ enum ElementVariant : int {
     kVarPersistent = 5,  // k_element_tma: persistent, state by bulk copies
     kVarColumns = 6,     // k_element_cols: one thread per column (elastic)
     kVarColumnsStaged = 7,  // k_element_cols with the block's stress staged by bulk copy
+    kVarColumnsPair = 8,    // k_element_cols2: two simulations per column thread (even-batch elastic)
     kVarCount
 };
 

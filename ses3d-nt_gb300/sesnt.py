@@ -37,7 +37,7 @@ FLAG_NO_STAGE = 256
 FLAG_AUTOTUNE = 512
 FLAG_FORCE64 = 1024
 (ELEMENT_AUTO, ELEMENT_POINT, ELEMENT_PAIR, ELEMENT_STAGE, ELEMENT_STAGE_REG, ELEMENT_PERSISTENT, ELEMENT_COLUMNS,
- ELEMENT_COLUMNS_STAGED) = range(8)
+ ELEMENT_COLUMNS_STAGED, ELEMENT_COLUMNS_PAIR) = range(9)
 SOURCE_MT, SOURCE_SF = 0, 1
 WAVELETS = {"DELTA": 0, "RICKER": 1, "GAUSS": 2, "SIN**3": 3, "BRUNE": 4}
 CH_VX, CH_VY, CH_VZ, CH_N = 1, 2, 4, 8

@@ -4,8 +4,8 @@ of the handle's error word (no device assert, no trap), which the next
 synchronising call returns as SESNT_ERANGE. This is the stand-in for a
 memory sanitizer: the library is rebuilt with the checks, and a subprocess
 runs every kernel variant (degrees 2-7, elastic and SLS, anisotropy,
-batches, FP32 and FP64, the staged, persistent, column and tensor-core
-element kernels, the tuner's sweep, strain and rotation state, every receiver
+batches, FP32 and FP64, the staged, persistent, column (one and two
+simulations per thread) and tensor-core element kernels, the tuner's sweep, strain and rotation state, every receiver
 channel, snapshot fields, the kinetic energy) on small grids."""
 import os
 import subprocess
@@ -29,6 +29,7 @@ from test_gpu_parity import small_workload, with_grid
 
 ALL = 0xFFFF
 C, CS, SR = sesnt.ELEMENT_COLUMNS, sesnt.ELEMENT_COLUMNS_STAGED, sesnt.ELEMENT_STAGE_REG
+CP = sesnt.ELEMENT_COLUMNS_PAIR
 cases = [  # lpd, n_sls, aniso, kind, flags, batch[, (variant, arg, piece) or "tune"[, precision]]
     (2, 0, False, sesnt.SOURCE_MT, 0, 1),
     (3, 3, False, sesnt.SOURCE_SF, 0, 2),
@@ -54,6 +55,9 @@ cases = [  # lpd, n_sls, aniso, kind, flags, batch[, (variant, arg, piece) or "t
     (4, 0, False, sesnt.SOURCE_SF, sesnt.FLAG_FORCE64, 4, (C, 1, 0)),
     (4, 3, True, sesnt.SOURCE_MT, 0, 3, (sesnt.ELEMENT_STAGE, 7, 0)),
     (6, 3, False, sesnt.SOURCE_MT, 0, 1, (SR, 6, 8192), 8),
+    (4, 0, False, sesnt.SOURCE_MT, 0, 4, (CP, 9, 0)),
+    (7, 0, True, sesnt.SOURCE_SF, 0, 2, (CP, 0, 0)),
+    (3, 0, False, sesnt.SOURCE_MT, 0, 6, (CP, 10, 0), 8),
 ]
 for case in cases:
     lpd, n_sls, aniso, kind, flags, batch = case[:6]
@@ -104,4 +108,4 @@ def test_every_kernel_in_bounds(gpu, tmp_path):
     code = SCRIPT % (PKG, HERE, str(tmp_path))
     r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=900)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
-    assert "OK 24" in r.stdout
+    assert "OK 27" in r.stdout

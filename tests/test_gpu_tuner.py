@@ -1,10 +1,11 @@
 """Element-kernel variants and the tuner, through the C ABI.
 
 - The column kernel (one thread per (i, j) column, z contractions in
-  registers) computes the step of the one-thread-per-point kernel: FP64 to
-  1e-12 relative L2, FP32 to 1e-5 (the order of the atomic adds differs), for
-  every degree, with and without anisotropy, in batches; and it matches the
-  oracle within the FP32 bound 1e-4.
+  registers) and its two-simulations-per-thread form compute the step of the
+  one-thread-per-point kernel: FP64 to 1e-12 relative L2, FP32 to 1e-5 (the
+  order of the atomic adds differs), for every degree, with and without
+  anisotropy, in batches; and the column kernel matches the oracle within the
+  FP32 bound 1e-4.
 - sesnt_tune keeps one of the variants that compute the step; the tuned
   handle's seismograms and wavefield equal the default handle's (FP32 to
   1e-5, FP64 to 1e-12); the choice is cached per GPU and grid and reused by
@@ -61,6 +62,29 @@ def test_column_kernel_matches_point_kernel(gpu, sesnt_lib, lpd, precision):
                       % (lpd, precision, aniso, batch, kname, arg, e, ev))
                 assert np.abs(sp).max() > 0
                 assert e < tol and ev < tol
+
+
+@pytest.mark.parametrize("lpd", [2, 3, 4, 5, 6, 7])
+@pytest.mark.parametrize("precision", [4, 8])
+def test_paired_column_kernel_matches_point_kernel(gpu, sesnt_lib, lpd, precision):
+    tol = 1e-5 if precision == 4 else 1e-12
+    for aniso, batch in ((False, 2), (True, 4), (False, 6)):
+        wl = batch_of(with_grid(small_workload(lpd, aniso=aniso, nt=120), precision=precision), batch)
+        sp, vp, name_p, _, _ = run(wl, 120, sesnt.ELEMENT_POINT)
+        assert name_p == "k_element"
+        for arg in ((0, 1, 2, 3, 8, 9, 10) if precision == 4 else (0, 8)):
+            sc, vcol, name_c, choice, _ = run(wl, 120, sesnt.ELEMENT_COLUMNS_PAIR, arg)
+            assert name_c == "k_element_cols2" and choice[:2] == (sesnt.ELEMENT_COLUMNS_PAIR, arg)
+            e = [rel_l2(sc[s], sp[s]) for s in range(batch)]
+            ev = rel_l2(vcol, vp)
+            print("lpd %d prec %d aniso %d batch %d arg %d: paired columns vs point seismograms %.2e, vz %.2e"
+                  % (lpd, precision, aniso, batch, arg, max(e), ev))
+            assert all(np.abs(sp[s]).max() > 0 for s in range(batch))
+            assert max(e) < tol and ev < tol
+    # an odd batch has no simulation pairs: the launch rules' kernel runs
+    wl = batch_of(with_grid(small_workload(lpd, nt=20), precision=precision), 3)
+    _, _, name, choice, _ = run(wl, 20, sesnt.ELEMENT_COLUMNS_PAIR, 0)
+    assert name == "k_element" and choice[0] == sesnt.ELEMENT_COLUMNS_PAIR
 
 
 @pytest.mark.parametrize("lpd", [4, 5, 6, 7])

@@ -4,15 +4,16 @@
 // unit's P*P threads own its columns: a thread keeps its column's velocity
 // (3 x P values) and its z-direction fluxes (3 x P) in registers, so the
 // z line contractions of the strain (src/evolution.f90:136-144) and of the
-// weak divergence (:350-356) read no shared memory. Only the x and y
+// weak divergence (:350-356) read no shared memory: their derivative-table
+// entries have compile-time indices and are read from the launch parameters
+// (StepArgs::tabz) as constant-bank operands. Only the x and y
 // contractions go through per-unit slabs: per point and simulation that is
 // 3 velocity stores + 30 loads and 6 flux stores + 30 loads, against 12
 // stores + 90 loads with one thread per point (k_element, k_element_pair),
 // whose batched elastic launches were bound by the shared-memory data pipe
 // (L1 90% busy, 36 M wavefronts on the 12x12x8 grid with 64 simulations).
 // The derivative-table columns a thread contracts with (x and y, strain and
-// divergence) sit in registers; the z ones are uniform across the block and
-// are read as shared-memory broadcasts. Per point, the arithmetic and its
+// divergence) sit in registers. Per point, the arithmetic and its
 // order are those of k_element (strain_contract, point_stress,
 // point_divergence).
 #pragma once
@@ -22,6 +23,7 @@ namespace sesnt {
 template <int N>
 struct ColCfg {
     static constexpr int P = N + 1, PP = P * P, NP = P * P * P;
+    static_assert(PP <= 64, "the z tables of the launch parameters hold 64 values");
     // units per block: as many whole columns sets as fit 128 threads
     static constexpr int G = PP <= 128 ? 128 / PP : 1;
     static constexpr int NT = ((G * PP + 31) / 32) * 32;
@@ -176,7 +178,7 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols(const Step
     __syncthreads();  // tables, velocity slabs and the mbarrier's initialisation
     bool landed = true;
     if constexpr (STAGE) landed = tma_try_wait(tma_smem(mbar), 0, a.wait_polls);
-    const T *Dx = sD, *Dy = sD + PP, *Dz = sD + 2 * PP, *Dt = sD + 3 * PP;
+    const T *Dx = sD, *Dy = sD + PP, *Dt = sD + 3 * PP;  // z tables: a.tabz (compile-time indices)
     T dxi[P], dyj[P];
 #pragma unroll
     for (int q = 0; q < P; ++q) {
@@ -201,7 +203,7 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols(const Step
             const T *col = sv + i + PP * k;       // y line (i, q, k)
 #pragma unroll
             for (int q = 0; q < P; ++q) {
-                const T dx = dxi[q], dy = dyj[q], dz = Dz[q * P + k];
+                const T dx = dxi[q], dy = dyj[q], dz = a.tabz[0][q * P + k];
                 ev[0] += row[q] * dx;
                 ev[1] += row[NP + q] * dx;
                 ev[2] += row[2 * NP + q] * dx;
@@ -250,7 +252,7 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols(const Step
             const T *col = sy + i + PP * k;
 #pragma unroll
             for (int q = 0; q < P; ++q) {
-                const T di = dti[q], dj = dtj[q], dk = Dt[k * P + q];
+                const T di = dti[q], dj = dtj[q], dk = a.tabz[1][k * P + q];
                 fx += zf[0][q] * dk + col[P * q] * dj + row[q] * di;
                 fy += zf[1][q] * dk + col[NP + P * q] * dj + row[NP + q] * di;
                 fz += zf[2][q] * dk + col[2 * NP + P * q] * dj + row[2 * NP + q] * di;
@@ -397,7 +399,7 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols2(const Ste
     };
     if (act) load_point(0, lam, mu, cA, cB, cC, sg);
     __syncthreads();  // tables and velocity slabs
-    const T *Dx = sD, *Dy = sD + PP, *Dz = sD + 2 * PP, *Dt = sD + 3 * PP;
+    const T *Dx = sD, *Dy = sD + PP, *Dt = sD + 3 * PP;  // z tables: a.tabz (compile-time indices)
     T dxi[P], dyj[P];
 #pragma unroll
     for (int q = 0; q < P; ++q) {
@@ -418,7 +420,7 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols2(const Ste
             const V *col = sv + i + PP * k;       // y line (i, q, k)
 #pragma unroll
             for (int q = 0; q < P; ++q) {
-                const T dx = dxi[q], dy = dyj[q], dz = Dz[q * P + k];
+                const T dx = dxi[q], dy = dyj[q], dz = a.tabz[0][q * P + k];
                 const V rx = row[q], ry = row[NP + q], rz = row[2 * NP + q];
                 const V cx = col[P * q], cy = col[NP + P * q], cz = col[2 * NP + P * q];
                 e0[0] += rx.x * dx;
@@ -509,7 +511,7 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols2(const Ste
         const V *col = sy + i + PP * k;
 #pragma unroll
         for (int q = 0; q < P; ++q) {
-            const T di = dti[q], dj = dtj[q], dk = Dt[k * P + q];
+            const T di = dti[q], dj = dtj[q], dk = a.tabz[1][k * P + q];
             const V r0 = row[q], r1 = row[NP + q], r2 = row[2 * NP + q];
             const V c0 = col[P * q], c1 = col[NP + P * q], c2 = col[2 * NP + P * q];
             f[0][0] += zf[0][0][q] * dk + c0.x * dj + r0.x * di;

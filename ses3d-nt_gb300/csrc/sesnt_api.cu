@@ -331,6 +331,7 @@ struct sesnt_handle {
     size_t dev_bytes = 0;
     // device buffers (typed by precision)
     void *tabD = nullptr, *w = nullptr, *sin_t = nullptr, *cot_t = nullptr, *r = nullptr;
+    double tabz[2][64] = {};  // host copy of Dz | Dt (rounded to the working precision)
     void *inv_r = nullptr, *inv_sin = nullptr;
     void *px = nullptr, *py = nullptr, *pz = nullptr;
     double *dsin = nullptr, *dr = nullptr, *dw = nullptr;
@@ -540,6 +541,10 @@ struct sesnt_handle {
             a.mem_drive[q] = (T)(dt / (kNsls * kTauP[q]));
         }
         a.inv_r = (const T *)inv_r; a.inv_sin = (const T *)inv_sin;
+        for (int q = 0; q < 64; ++q) {
+            a.tabz[0][q] = (T)tabz[0][q];
+            a.tabz[1][q] = (T)tabz[1][q];
+        }
         a.tabD = (const T *)tabD; a.w = (const T *)w; a.sin_t = (const T *)sin_t; a.cot_t = (const T *)cot_t;
         a.r = (const T *)r; a.px = (const T *)px; a.py = (const T *)py; a.pz = (const T *)pz;
         a.lam = (const T *)lam; a.mu = (const T *)mu; a.A = (const T *)A; a.B = (const T *)B; a.C = (const T *)C;
@@ -704,6 +709,10 @@ int setup_tables(sesnt_t *h) {
     }
     std::vector<T> pxv, pyv, pzv;
     taper_profiles<T>(g.nx, g.ny, g.nz, N, g.taper_width, (T)g.taper_slope, d, pxv, pyv, pzv);
+    for (int x = 0; x < P * P; ++x) {
+        h->tabz[0][x] = (double)tab[2 * P * P + x];
+        h->tabz[1][x] = (double)tab[3 * P * P + x];
+    }
     int rc;
     if ((rc = upload(h, h->tabD, tab, "tables"))) return rc;
     if ((rc = upload(h, h->w, wt, "weights"))) return rc;

@@ -76,6 +76,9 @@ struct StepArgs {
     T mem_drive[kNsls];  // dt/(n_sls*tau_p(k))
     // small tables (device): tabD = [Dx | Dy | Dz | Dt], each P*P
     const T *tabD, *w, *sin_t, *cot_t, *r, *px, *py, *pz;
+    // Dz and Dt again in the launch parameters (constant bank), for kernels
+    // that index them with compile-time indices only (the column kernels)
+    T tabz[2][64];
     const T *inv_r, *inv_sin;  // 1/r [nz*P], 1/sin(theta) [nx*P]
     // model (element-local)
     const T *lam, *mu, *A, *B, *C, *tau;

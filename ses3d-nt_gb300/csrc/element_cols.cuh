@@ -187,6 +187,16 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols(const Step
     }
     T zf[3][P];  // z fluxes of this column: xz, yz, zz weighted (contracted along k)
     const T m0[6][1] = {{0}, {0}, {0}, {0}, {0}, {0}};
+    // the column's metric values that do not change along k, loaded once
+    PointMetric<T> pm{};
+    if (act) {
+        pm.ct = a.cot_t[ex * P + i];
+        pm.isn = a.inv_sin[ex * P + i];
+        pm.st = a.sin_t[ex * P + i];
+        pm.px = a.px[ex * P + i];
+        pm.py = a.py[ey * P + j];
+        pm.wij = a.w[i] * a.w[j];
+    }
 #pragma unroll
     for (int k = 0; k < P; ++k) {
         T nlam = 0, nmu = 0, nA = 0, nB = 0, nC = 0, nsg[6] = {0, 0, 0, 0, 0, 0};
@@ -215,9 +225,13 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols(const Step
                 ev[8] += vc[2][q] * dz;
             }
             T sn[6], gw[3];
-            point_stress<N, T, 0, ANISO, false, STAGE>(a, ev, vc[0][k], vc[1][k], vc[2][k], i, j, k, ex, ey, ez, lam,
-                                                       mu, T(0), cA, cB, cC, sg, m0, sig + PP * k, nullptr, NPS, nloc,
-                                                       nullptr, sn, gw);
+            pm.ir = a.inv_r[ez * P + k];
+            pm.rr = a.r[ez * P + k];
+            pm.pz = a.pz[ez * P + k];
+            pm.wk = a.w[k];
+            point_stress<N, T, 0, ANISO, false, STAGE, true>(a, ev, vc[0][k], vc[1][k], vc[2][k], i, j, k, ex, ey, ez,
+                                                             lam, mu, T(0), cA, cB, cC, sg, m0, sig + PP * k, nullptr,
+                                                             NPS, nloc, nullptr, sn, gw, &pm);
             const int p = c + PP * k;
             sx[p] = sn[0] * gw[0];
             sx[NP + p] = sn[1] * gw[0];
@@ -408,6 +422,16 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols2(const Ste
     }
     T zf[2][3][P];  // z fluxes of the column (xz, yz, zz weighted), both simulations
     const T m0[6][1] = {{0}, {0}, {0}, {0}, {0}, {0}};
+    // the column's metric values that do not change along k, loaded once
+    T ct = 0, isn = 0, st = 0, pxv = 0, pyv = 0, wij = 0;
+    if (act) {
+        ct = a.cot_t[ex * P + i];
+        isn = a.inv_sin[ex * P + i];
+        st = a.sin_t[ex * P + i];
+        pxv = a.px[ex * P + i];
+        pyv = a.py[ey * P + j];
+        wij = a.w[i] * a.w[j];
+    }
 #pragma unroll
     for (int k = 0; k < P; ++k) {
         T nlam = 0, nmu = 0, nA = 0, nB = 0, nC = 0, nsg[2][6] = {{0, 0, 0, 0, 0, 0}, {0, 0, 0, 0, 0, 0}};
@@ -442,13 +466,14 @@ __global__ void __launch_bounds__(ColCfg<N>::NT, MINB) k_element_cols2(const Ste
                 e1[7] += vc[1][1][q] * dz;
                 e1[8] += vc[1][2][q] * dz;
             }
+            const T ir = a.inv_r[ez * P + k], irs = ir * isn;
             T g0[9], g1[9];
-            complete_gradient<N, T>(a, e0, vc[0][0][k], vc[0][1][k], vc[0][2][k], i, k, ex, ez, g0);
-            complete_gradient<N, T>(a, e1, vc[1][0][k], vc[1][1][k], vc[1][2][k], i, k, ex, ez, g1);
-            const T tp = taper_value(a.px[ex * P + i], a.py[ey * P + j], a.pz[ez * P + k], a.inv_alpha);
+            complete_gradient_m<T>(e0, vc[0][0][k], vc[0][1][k], vc[0][2][k], ir, ct, irs, g0);
+            complete_gradient_m<T>(e1, vc[1][0][k], vc[1][1][k], vc[1][2][k], ir, ct, irs, g1);
+            const T tp = taper_value(pxv, pyv, a.pz[ez * P + k], a.inv_alpha);
             const T rr = a.r[ez * P + k];
-            const T rs = rr * a.sin_t[ex * P + i];
-            const T W = a.w[i] * a.w[j] * a.w[k];
+            const T rs = rr * st;
+            const T W = wij * a.w[k];
             const T gx = W * rs * a.c1, gy = W * rr * a.c2, gz = W * (rr * rs) * a.c3;
             T sn[2][6];  // integrated stress before the taper: xx xy xz yy yz zz
             auto update = [&](const T(&gg)[9], const T(&sgv)[6], T *sig, T(&o)[6]) {

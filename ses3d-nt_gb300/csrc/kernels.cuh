@@ -195,14 +195,12 @@ __device__ __forceinline__ void strain_contract(const T *sD, const T *svx, const
 // (src/evolution.f90:165-173; theta = x, phi = y, r = z). Divisions by r and
 // r*sin(theta) are products with tabulated reciprocals. Output g[9] in the
 // order kDu* (xx yy zz xy yx xz zx yz zy), not yet symmetrised.
-template <int N, typename T>
-__device__ __forceinline__ void complete_gradient(const StepArgs<T> &a, const T (&e)[9], T vx, T vy, T vz, int i,
-                                                  int k, int ex, int ez, T (&g)[9]) {
-    constexpr int P = N + 1;
+// The completion from the point's metric values: ir = 1/r, ct = cot(theta),
+// irs = 1/(r sin(theta)).
+template <typename T>
+__device__ __forceinline__ void complete_gradient_m(const T (&e)[9], T vx, T vy, T vz, T ir, T ct, T irs,
+                                                    T (&g)[9]) {
     T exx = e[0], exy = e[1], exz = e[2], eyx = e[3], eyy = e[4], eyz = e[5], ezx = e[6], ezy = e[7], ezz = e[8];
-    const T ir = a.inv_r[ez * P + k];
-    const T ct = a.cot_t[ex * P + i];
-    const T irs = ir * a.inv_sin[ex * P + i];
     ezz = -ezz;
     eyy = eyy * irs + (vz + vx * ct) * ir;
     exx = (vz + exx) * ir;
@@ -216,6 +214,24 @@ __device__ __forceinline__ void complete_gradient(const StepArgs<T> &a, const T 
     g[kDuXY] = exy; g[kDuYX] = eyx; g[kDuXZ] = exz;
     g[kDuZX] = ezx; g[kDuYZ] = eyz; g[kDuZY] = ezy;
 }
+
+template <int N, typename T>
+__device__ __forceinline__ void complete_gradient(const StepArgs<T> &a, const T (&e)[9], T vx, T vy, T vz, int i,
+                                                  int k, int ex, int ez, T (&g)[9]) {
+    constexpr int P = N + 1;
+    const T ir = a.inv_r[ez * P + k];
+    const T ct = a.cot_t[ex * P + i];
+    const T irs = ir * a.inv_sin[ex * P + i];
+    complete_gradient_m<T>(e, vx, vy, vz, ir, ct, irs, g);
+}
+
+// Metric values of one point that a caller has already loaded (the column
+// kernels hold the column-invariant ones in registers): 1/r, cot(theta),
+// 1/sin(theta), r, sin(theta), the three taper profiles, w_i * w_j and w_k.
+template <typename T>
+struct PointMetric {
+    T ir, ct, isn, rr, st, px, py, pz, wij, wk;
+};
 
 // Stress rates from the symmetrised strain rates (src/evolution.f90:287-296),
 // or the standard-linear-solid form with the memory variables m
@@ -274,18 +290,27 @@ __device__ __forceinline__ void stress_rates(T exx, T eyy, T ezz, T exy, T exz, 
 // compile-time switch, since even a skipped branch measured 1.5% on the
 // step. SMEM: sig/mem point into shared memory (plain stores instead of
 // streaming global stores).
-template <int N, typename T, int NSLS, bool ANISO, bool DU = false, bool SMEM = false>
+// PM: the metric values come from *pm (PointMetric) instead of the tables.
+template <int N, typename T, int NSLS, bool ANISO, bool DU = false, bool SMEM = false, bool PM = false>
 __device__ __forceinline__ void point_stress(const StepArgs<T> &a, const T (&e)[9], T vx, T vy, T vz, int i, int j,
                                              int k, int ex, int ey, int ez, T lam, T mu, T tau, T cA, T cB, T cC,
                                              const T (&sg)[6], const T (&m)[6][NSLS > 0 ? NSLS : 1], T *sig, T *mem,
-                                             size_t cs, size_t nloc, T *du, T (&sn)[6], T (&gw)[3]) {
+                                             size_t cs, size_t nloc, T *du, T (&sn)[6], T (&gw)[3],
+                                             const PointMetric<T> *pm = nullptr) {
     constexpr int P = N + 1;
     T g[9];
-    complete_gradient<N, T>(a, e, vx, vy, vz, i, k, ex, ez, g);
+    if constexpr (PM) complete_gradient_m<T>(e, vx, vy, vz, pm->ir, pm->ct, pm->ir * pm->isn, g);
+    else complete_gradient<N, T>(a, e, vx, vy, vz, i, k, ex, ez, g);
     T exx = g[kDuXX], eyy = g[kDuYY], ezz = g[kDuZZ], exy = g[kDuXY], eyx = g[kDuYX], exz = g[kDuXZ],
       ezx = g[kDuZX], eyz = g[kDuYZ], ezy = g[kDuZY];
-    const T rr = a.r[ez * P + k];
-    const T rs = rr * a.sin_t[ex * P + i];
+    T rr, rs;
+    if constexpr (PM) {
+        rr = pm->rr;
+        rs = rr * pm->st;
+    } else {
+        rr = a.r[ez * P + k];
+        rs = rr * a.sin_t[ex * P + i];
+    }
     if constexpr (DU) {
         // displacement gradient du += dt * (completed velocity gradient)
         // before the symmetrisation (src/evolution.f90:179-187)
@@ -306,7 +331,8 @@ __device__ __forceinline__ void point_stress(const StepArgs<T> &a, const T (&e)[
     const T syy = sg[3] + a.dt * ryy;
     const T syz = sg[4] + a.dt * ryz;
     const T szz = sg[5] + a.dt * rzz;
-    const T tp = taper_value(a.px[ex * P + i], a.py[ey * P + j], a.pz[ez * P + k], a.inv_alpha);
+    const T tp = PM ? taper_value(pm->px, pm->py, pm->pz, a.inv_alpha)
+                    : taper_value(a.px[ex * P + i], a.py[ey * P + j], a.pz[ez * P + k], a.inv_alpha);
     auto put = [](T *q, T v) {
         if constexpr (SMEM) *q = v;
         else st_stream(q, v);
@@ -337,7 +363,7 @@ __device__ __forceinline__ void point_stress(const StepArgs<T> &a, const T (&e)[
         }
     }
     // metric weights of the stresses in the weak divergence
-    const T W = a.w[i] * a.w[j] * a.w[k];
+    const T W = PM ? pm->wij * pm->wk : a.w[i] * a.w[j] * a.w[k];
     gw[0] = W * rs * a.c1;
     gw[1] = W * rr * a.c2;
     gw[2] = W * (rr * rs) * a.c3;

@@ -26,7 +26,7 @@
   error of a wavefield is set by rounding (both the GPU and the oracle sit
   near 1e-4 of FP64 there).
 
-Tolerances: 1e-4 relative L2 for FP32 results (the benchmark spec's bound), 1e-3
+Tolerances: 1e-4 relative L2 for FP32 results (the required FP32 misfit), 1e-3
 for the BF16x3 contractions (a split into three bfloat16 products keeps about
 16 significant bits per product), 1e-10 for FP64 wavefields against the FP64
 oracle, float32 output rounding (1e-7) for FP64 seismograms.

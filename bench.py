@@ -269,6 +269,8 @@ def run_ours(args):
                 "tc_bf16x3": sesnt.FLAG_TC_BF16X3, "unstaged": sesnt.FLAG_NO_STAGE}.get(args.element, 0)
     if args.force64:
         g.flags |= sesnt.FLAG_FORCE64
+    if args.kahan_stress:
+        g.flags |= sesnt.FLAG_KAHAN_STRESS
     S = g.batch
     hbm, peak_kind = peaks()
 
@@ -309,6 +311,7 @@ def run_ours(args):
                          % (info["algorithmic_bytes_per_step"] / 1e9),
                    "graph": not (g.flags & sesnt.FLAG_NO_GRAPH), "element": args.element,
                    "force_assembly": "fp64" if args.force64 else "fp32",
+                   "stress_integration": "compensated" if args.kahan_stress else "plain",
                    "element_kernel": {"name": kname, "variant": choice[0], "arg": choice[1], "piece": choice[2],
                                       "tuning": tune_report.strip().splitlines()[1:] if tune_report else None},
                    "parallelism": "replicas" if WORLD > 1 else "single GPU"},
@@ -460,8 +463,9 @@ def batched_headline(args):
 
 
 def accuracy(args, wl):
-    """FP32 (plain, Kahan-compensated velocity update, force assembled in
-    FP64, tensor-core contractions) against the FP64 build of the same
+    """FP32 (plain, Kahan-compensated velocity update, compensated stress
+    integration, both, force assembled in FP64, tensor-core contractions) against
+    the FP64 build of the same
     kernels: relative L2 of the seismograms of the first simulation and of
     its final vz after accuracy_steps steps."""
     import numpy as np
@@ -471,6 +475,8 @@ def accuracy(args, wl):
     n = min(args.accuracy_steps, wl.grid.nt)
     res = {}
     for name, prec, flags in (("fp32", 4, 0), ("fp32_kahan", 4, sesnt.FLAG_KAHAN),
+                              ("fp32_kahan_stress", 4, sesnt.FLAG_KAHAN_STRESS),
+                              ("fp32_kahan_stress_and_v", 4, sesnt.FLAG_KAHAN_STRESS | sesnt.FLAG_KAHAN),
                               ("fp32_force64", 4, sesnt.FLAG_FORCE64),
                               ("fp32_tc_tf32x3", 4, sesnt.FLAG_TC_TF32X3),
                               ("fp32_tc_bf16x3", 4, sesnt.FLAG_TC_BF16X3), ("fp64", 8, 0)):
@@ -486,7 +492,8 @@ def accuracy(args, wl):
             res[name] = (sim.seismograms()[0].astype(np.float64), sim.field("vz", precision=8))
     rel = lambda a, b: float(np.linalg.norm(a - b) / np.linalg.norm(b))
     out = {"steps": n}
-    for name in ("fp32", "fp32_kahan", "fp32_force64", "fp32_tc_tf32x3", "fp32_tc_bf16x3"):
+    for name in ("fp32", "fp32_kahan", "fp32_kahan_stress", "fp32_kahan_stress_and_v", "fp32_force64",
+                 "fp32_tc_tf32x3", "fp32_tc_bf16x3"):
         out[name] = {"seismogram_rel_l2": rel(res[name][0], res["fp64"][0]),
                      "vz_rel_l2": rel(res[name][1], res["fp64"][1])}
     return out
@@ -672,6 +679,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-seconds", type=float, default=60.0)
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
+    ap.add_argument("--kahan-stress", action="store_true",
+                    help="compensated stress integration (SESNT_FLAG_KAHAN_STRESS) in the measured run")
     ap.add_argument("--force64", action="store_true",
                     help="assemble the force in FP64 (SESNT_FLAG_FORCE64) in the measured run")
     ap.add_argument("--no-batched", dest="batched", action="store_false",

@@ -67,6 +67,12 @@ extern "C" {
                                      are available after the steps of a rotation snapshot) */
 #define SESNT_FLAG_AUTOTUNE 512u  /* sesnt_set_model applies the tuning cache's choice for this GPU
                                      and grid, or runs sesnt_tune and caches its choice */
+#define SESNT_FLAG_KAHAN_STRESS 2048u /* compensated (Kahan) stress integration: six compensation
+                                         terms per point carry what the stored stress loses to
+                                         rounding at each step, the dominant FP32 error against FP64
+                                         over long runs; +48 bytes per point and step. Runs the
+                                         staged kernel (SLS, degrees 4-7) or one point per thread;
+                                         not with the tensor-core, persistent or strain flags */
 #define SESNT_FLAG_FORCE64 1024u  /* FP32 wavefields: assemble the force of shared points in FP64
                                      (FP64 atomic adds, 12 more bytes per unique point and step);
                                      FP64 handles already do */

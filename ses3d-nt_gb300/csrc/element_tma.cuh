@@ -292,8 +292,11 @@ struct StageCfg {
     static constexpr int MINB = sizeof(T) == 4 ? (NT <= 128 ? SESNT_MINB_STAGE : ElemCfg<N>::MINB) : 1;
 };
 
-template <int N, typename T, int NSLS, bool ANISO, bool STORE>
+// KS: compensated stress integration (SESNT_FLAG_KAHAN_STRESS), register
+// stores only; each thread loads and stores its point's compensation terms.
+template <int N, typename T, int NSLS, bool ANISO, bool STORE, bool KS = false>
 __global__ void __launch_bounds__(StageCfg<N, T, NSLS>::NT, StageCfg<N, T, NSLS>::MINB) k_element_stage(const StepArgs<T> a) {
+    static_assert(!(STORE && KS), "compensated stress integration stores from registers");
     using C = StageCfg<N, T, NSLS>;
     constexpr int P = C::P, NP = C::NP, NPS = C::NPS, NT = C::NT, MS = NSLS > 0 ? NSLS : 1;
     extern __shared__ __align__(128) unsigned char stage_smem_raw[];
@@ -381,9 +384,10 @@ __global__ void __launch_bounds__(StageCfg<N, T, NSLS>::NT, StageCfg<N, T, NSLS>
                                                          cB, cC, sg, m, st + p, st + 6 * NPS + p, NPS, nloc, sf,
                                                          nullptr);
         else
-            point_update<N, T, NSLS, ANISO>(a, ev, vx, vy, vz, p, i, j, k, ex, ey, ez, lam, mu, tau, cA, cB, cC, sg,
-                                            m, a.sig + sb * C::UNIT + p, a.mem + sb * C::UNIT + p, NPS, nloc, sf,
-                                            nullptr);
+            point_update<N, T, NSLS, ANISO, false, false, KS>(a, ev, vx, vy, vz, p, i, j, k, ex, ey, ez, lam, mu, tau,
+                                                              cA, cB, cC, sg, m, a.sig + sb * C::UNIT + p,
+                                                              a.mem + sb * C::UNIT + p, NPS, nloc, sf, nullptr,
+                                                              KS ? a.sigc + sb * 6 * NPS + p : nullptr);
     }
     // updated state in the stage: visible to the bulk-copy engine after the barrier
     if constexpr (STORE) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -411,7 +415,8 @@ int prepare_element_stage() {
     using C = StageCfg<N, T, NSLS>;
     if (C::SMEM <= 48 * 1024) return 0;
     if (C::SMEM > kMaxSmemPerBlock) return 0;
-    for (auto *f : {k_element_stage<N, T, NSLS, ANISO, true>, k_element_stage<N, T, NSLS, ANISO, false>})
+    for (auto *f : {k_element_stage<N, T, NSLS, ANISO, true>, k_element_stage<N, T, NSLS, ANISO, false>,
+                    k_element_stage<N, T, NSLS, ANISO, false, true>})
         if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)C::SMEM) != cudaSuccess)
             return -1;
     return 0;
@@ -423,7 +428,9 @@ int launch_element_stage(const StepArgs<T> &a, int store, void *stream) {
     using C = StageCfg<N, T, NSLS>;
     if (C::SMEM > kMaxSmemPerBlock) return 1;
     const long long blocks = (long long)a.nel * a.S;
-    if (store < 0 ? C::STORE_DEFAULT : store != 0)
+    if (a.sigc)
+        k_element_stage<N, T, NSLS, ANISO, false, true><<<(unsigned)blocks, C::NT, C::SMEM, (cudaStream_t)stream>>>(a);
+    else if (store < 0 ? C::STORE_DEFAULT : store != 0)
         k_element_stage<N, T, NSLS, ANISO, true><<<(unsigned)blocks, C::NT, C::SMEM, (cudaStream_t)stream>>>(a);
     else
         k_element_stage<N, T, NSLS, ANISO, false><<<(unsigned)blocks, C::NT, C::SMEM, (cudaStream_t)stream>>>(a);

@@ -291,12 +291,17 @@ __device__ __forceinline__ void stress_rates(T exx, T eyy, T ezz, T exy, T exz, 
 // step. SMEM: sig/mem point into shared memory (plain stores instead of
 // streaming global stores).
 // PM: the metric values come from *pm (PointMetric) instead of the tables.
-template <int N, typename T, int NSLS, bool ANISO, bool DU = false, bool SMEM = false, bool PM = false>
+// KS: compensated (Kahan) stress integration (SESNT_FLAG_KAHAN_STRESS): sigc
+// points to the point's six compensation terms (global memory, stride cs),
+// which carry the low-order part the FP32 stress loses at each step. The
+// compensation is tapered with the stress.
+template <int N, typename T, int NSLS, bool ANISO, bool DU = false, bool SMEM = false, bool PM = false,
+          bool KS = false>
 __device__ __forceinline__ void point_stress(const StepArgs<T> &a, const T (&e)[9], T vx, T vy, T vz, int i, int j,
                                              int k, int ex, int ey, int ez, T lam, T mu, T tau, T cA, T cB, T cC,
                                              const T (&sg)[6], const T (&m)[6][NSLS > 0 ? NSLS : 1], T *sig, T *mem,
                                              size_t cs, size_t nloc, T *du, T (&sn)[6], T (&gw)[3],
-                                             const PointMetric<T> *pm = nullptr) {
+                                             const PointMetric<T> *pm = nullptr, T *sigc = nullptr) {
     constexpr int P = N + 1;
     T g[9];
     if constexpr (PM) complete_gradient_m<T>(e, vx, vy, vz, pm->ir, pm->ct, pm->ir * pm->isn, g);
@@ -325,12 +330,27 @@ __device__ __forceinline__ void point_stress(const StepArgs<T> &a, const T (&e)[
     stress_rates<T, NSLS, ANISO>(exx, eyy, ezz, exy, exz, eyz, lam, mu, tau, cA, cB, cC, m, rxx, ryy, rzz, rxy, rxz,
                                  ryz);
     // integrate, taper the stored stress
-    const T sxx = sg[0] + a.dt * rxx;
-    const T sxy = sg[1] + a.dt * rxy;
-    const T sxz = sg[2] + a.dt * rxz;
-    const T syy = sg[3] + a.dt * ryy;
-    const T syz = sg[4] + a.dt * ryz;
-    const T szz = sg[5] + a.dt * rzz;
+    T sxx, sxy, sxz, syy, syz, szz, cn[6];
+    if constexpr (KS) {
+        // s + dt*r with the compensation c of the previous step: y = dt*r - c,
+        // t = s + y, new compensation (t - s) - y
+        const T r6[6] = {rxx, rxy, rxz, ryy, ryz, rzz};
+        T o[6];
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const T y = a.dt * r6[q] - ld_stream(sigc + q * cs);
+            o[q] = sg[q] + y;
+            cn[q] = (o[q] - sg[q]) - y;
+        }
+        sxx = o[0]; sxy = o[1]; sxz = o[2]; syy = o[3]; syz = o[4]; szz = o[5];
+    } else {
+        sxx = sg[0] + a.dt * rxx;
+        sxy = sg[1] + a.dt * rxy;
+        sxz = sg[2] + a.dt * rxz;
+        syy = sg[3] + a.dt * ryy;
+        syz = sg[4] + a.dt * ryz;
+        szz = sg[5] + a.dt * rzz;
+    }
     const T tp = PM ? taper_value(pm->px, pm->py, pm->pz, a.inv_alpha)
                     : taper_value(a.px[ex * P + i], a.py[ey * P + j], a.pz[ez * P + k], a.inv_alpha);
     auto put = [](T *q, T v) {
@@ -343,6 +363,10 @@ __device__ __forceinline__ void point_stress(const StepArgs<T> &a, const T (&e)[
     put(sig + 3 * cs, syy * tp);
     put(sig + 4 * cs, syz * tp);
     put(sig + 5 * cs, szz * tp);
+    if constexpr (KS) {
+#pragma unroll
+        for (int q = 0; q < 6; ++q) st_stream(sigc + q * cs, cn[q] * tp);
+    }
     if constexpr (NSLS > 0) {
         // memory variables after the update, driven by this step's rates:
         // M <- M - M*(dt/tau_p) - tau*dt/(n*tau_p)*e, the reference's form
@@ -373,15 +397,15 @@ __device__ __forceinline__ void point_stress(const StepArgs<T> &a, const T (&e)[
 // point_stress, then the metric-weighted stresses for the weak divergence
 // written to the flux slab `my` (9 x NP): entries 0, 3, 6 are contracted
 // along x, 1, 4, 7 along y, 2, 5, 8 along z (point_divergence).
-template <int N, typename T, int NSLS, bool ANISO, bool DU = false, bool SMEM = false>
+template <int N, typename T, int NSLS, bool ANISO, bool DU = false, bool SMEM = false, bool KS = false>
 __device__ __forceinline__ void point_update(const StepArgs<T> &a, const T (&e)[9], T vx, T vy, T vz, int p, int i,
                                              int j, int k, int ex, int ey, int ez, T lam, T mu, T tau, T cA, T cB,
                                              T cC, const T (&sg)[6], const T (&m)[6][NSLS > 0 ? NSLS : 1], T *sig,
-                                             T *mem, size_t cs, size_t nloc, T *my, T *du) {
+                                             T *mem, size_t cs, size_t nloc, T *my, T *du, T *sigc = nullptr) {
     constexpr int P = N + 1, NP = P * P * P;
     T sn[6], gw[3];
-    point_stress<N, T, NSLS, ANISO, DU, SMEM>(a, e, vx, vy, vz, i, j, k, ex, ey, ez, lam, mu, tau, cA, cB, cC, sg, m,
-                                              sig, mem, cs, nloc, du, sn, gw);
+    point_stress<N, T, NSLS, ANISO, DU, SMEM, false, KS>(a, e, vx, vy, vz, i, j, k, ex, ey, ez, lam, mu, tau, cA, cB,
+                                                         cC, sg, m, sig, mem, cs, nloc, du, sn, gw, nullptr, sigc);
     my[0 * NP + p] = sn[0] * gw[0];
     my[1 * NP + p] = sn[1] * gw[1];
     my[2 * NP + p] = sn[2] * gw[2];
@@ -394,16 +418,16 @@ __device__ __forceinline__ void point_update(const StepArgs<T> &a, const T (&e)[
 }
 
 // One element-local point of the step with CUDA-core contractions.
-template <int N, typename T, int NSLS, bool ANISO, bool DU = false>
+template <int N, typename T, int NSLS, bool ANISO, bool DU = false, bool KS = false>
 __device__ __forceinline__ void point_step(const StepArgs<T> &a, const T *sD, const T *svx, const T *svy,
                                            const T *svz, int p, int i, int j, int k, int ex, int ey, int ez,
                                            T lam, T mu, T tau, T cA, T cB, T cC, const T (&sg)[6],
                                            const T (&m)[6][NSLS > 0 ? NSLS : 1], T *sig, T *mem, size_t cs,
-                                           size_t nloc, T *my, T *du) {
+                                           size_t nloc, T *my, T *du, T *sigc = nullptr) {
     T e[9];
     strain_contract<N, T>(sD, svx, svy, svz, i, j, k, e);
-    point_update<N, T, NSLS, ANISO, DU>(a, e, svx[p], svy[p], svz[p], p, i, j, k, ex, ey, ez, lam, mu, tau, cA, cB,
-                                        cC, sg, m, sig, mem, cs, nloc, my, du);
+    point_update<N, T, NSLS, ANISO, DU, false, KS>(a, e, svx[p], svy[p], svz[p], p, i, j, k, ex, ey, ez, lam, mu, tau,
+                                                   cA, cB, cC, sg, m, sig, mem, cs, nloc, my, du, sigc);
 }
 
 // Weak divergence at point (i,j,k): transposed line contractions over the
@@ -430,7 +454,7 @@ __device__ __forceinline__ size_t unique_index(int NXU, int NYU, int ex, int ey,
 }
 
 // One block per group of EPB elements and simulation.
-template <int N, typename T, int NSLS, bool ANISO, bool DU>
+template <int N, typename T, int NSLS, bool ANISO, bool DU, bool KS = false>
 __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::MINB : 1) k_element(const StepArgs<T> a) {
     constexpr int P = ElemCfg<N>::P, NP = ElemCfg<N>::NP, EPB = ElemCfg<N>::EPB, NT = ElemCfg<N>::NT;
     constexpr int MS = NSLS > 0 ? NSLS : 1;
@@ -510,9 +534,10 @@ __global__ void __launch_bounds__(ElemCfg<N>::NT, sizeof(T) == 4 ? ElemCfg<N>::M
 #pragma unroll
                 for (int q = 0; q < NSLS; ++q) m[c][q] = ld_stream(mem + (size_t)(c * NSLS + q) * NPS);
         }
-        point_step<N, T, NSLS, ANISO, DU>(a, sD, svx, svx + NP, svx + 2 * NP, p, i, j, k, ex, ey, ez, lam, mu, tau,
-                                          cA, cB, cC, sg, m, sig, mem, NPS, nloc, sf + le * 9 * NP,
-                                          DU ? a.du + (size_t)s * 9 * nloc + li : nullptr);
+        point_step<N, T, NSLS, ANISO, DU, KS>(a, sD, svx, svx + NP, svx + 2 * NP, p, i, j, k, ex, ey, ez, lam, mu,
+                                              tau, cA, cB, cC, sg, m, sig, mem, NPS, nloc, sf + le * 9 * NP,
+                                              DU ? a.du + (size_t)s * 9 * nloc + li : nullptr,
+                                              KS ? a.sigc + sb * 6 * NPS + p : nullptr);
     }
     __syncthreads();
     if (act) {
@@ -969,6 +994,7 @@ int launch_element_v(const StepArgs<T> &a, void *stream) {
     }
     const size_t smem = sizeof(T) * (4 * C::P * C::P + C::EPB * 12 * C::NP);
     if (a.du) k_element<N, T, NSLS, ANISO, true><<<(unsigned)groups, C::NT, smem, (cudaStream_t)stream>>>(a);
+    else if (a.sigc) k_element<N, T, NSLS, ANISO, false, true><<<(unsigned)groups, C::NT, smem, (cudaStream_t)stream>>>(a);
     else k_element<N, T, NSLS, ANISO, false><<<(unsigned)groups, C::NT, smem, (cudaStream_t)stream>>>(a);
     return cudaPeekAtLastError() == cudaSuccess ? 0 : -1;
 }
@@ -984,6 +1010,9 @@ int prepare_variant() {
     if (e == cudaSuccess && smem > 48 * 1024)
         e = cudaFuncSetAttribute(k_element<N, T, NSLS, ANISO, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)smem);
+    if (e == cudaSuccess && smem > 48 * 1024)
+        e = cudaFuncSetAttribute(k_element<N, T, NSLS, ANISO, false, true>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if constexpr (NSLS == 0) {
         const size_t smem2 = sizeof(T) * (4 * C::P * C::P + C::EPB * 24 * C::NP);
         if (e == cudaSuccess && smem2 > 48 * 1024)
@@ -1087,6 +1116,9 @@ ElemKernel plan_element(const StepArgs<T> &a, bool sls, bool aniso) {
     if (std::is_same_v<T, float> && a.contraction) return ElemKernel::Tc;
     const bool even = a.S >= 2 && a.S % 2 == 0;
     if (a.du) return ElemKernel::Point;
+    // compensated stress integration: the staged kernel with register stores
+    // (SLS, degrees 4-7) or one point per thread
+    if (a.sigc) return sls && has_staged<N, T>() ? ElemKernel::StageReg : ElemKernel::Point;
     switch (a.variant) {
         case kVarPoint: return ElemKernel::Point;
         case kVarPair: if (!sls && even) return ElemKernel::Pair; break;

@@ -338,6 +338,7 @@ struct sesnt_handle {
     void *lam = nullptr, *mu = nullptr, *A = nullptr, *B = nullptr, *C = nullptr, *tau = nullptr;
     void *sig = nullptr, *mem = nullptr, *v = nullptr, *vc = nullptr, *F = nullptr, *invM = nullptr;
     double *F64 = nullptr;  // SESNT_FLAG_FORCE64 on FP32 handles: the force accumulated in FP64
+    void *sigc = nullptr;   // SESNT_FLAG_KAHAN_STRESS: stress compensation terms [units][6][CS]
     int *d_it = nullptr;
     int *d_err = nullptr;  // set by a kernel whose bounded wait ran out
     int wait_polls = 1 << 22, drop_completion = 0;
@@ -551,6 +552,7 @@ struct sesnt_handle {
         a.tau = (const T *)tau;
         a.sig = (T *)sig; a.mem = (T *)mem; a.v = (T *)v; a.vc = (T *)vc; a.F = (T *)F; a.invM = (const T *)invM;
         a.F64 = F64;
+        a.sigc = (T *)sigc;
         a.st_cs = state_cs(); a.st_unit = (long long)state_unit();
         a.nsrc = nsrc_rec; a.nt = g.nt; a.n_src_vm = n_src_vm; a.n_src_data = n_src_data; a.src = (const SrcRec *)d_src; a.src_vm = (const T *)d_src_vm;
         a.src_data = (const T *)d_src_data;
@@ -646,6 +648,11 @@ int check_grid(const sesnt_grid_t *g, std::string &why) {
     if ((g->flags & SESNT_FLAG_STRAIN) &&
         (g->flags & (SESNT_FLAG_TC_TF32X3 | SESNT_FLAG_TC_BF16X3 | SESNT_FLAG_PERSISTENT_ELEMENT))) {
         why = "the displacement gradient is built into the default element kernel only";
+        return SESNT_EUNSUPPORTED;
+    }
+    if ((g->flags & SESNT_FLAG_KAHAN_STRESS) && (g->flags & (SESNT_FLAG_TC_TF32X3 | SESNT_FLAG_TC_BF16X3 |
+                                                             SESNT_FLAG_PERSISTENT_ELEMENT | SESNT_FLAG_STRAIN))) {
+        why = "compensated stress integration is built into the staged and one-point-per-thread kernels only";
         return SESNT_EUNSUPPORTED;
     }
     if (g->batch < 1) return bad("batch must be >= 1");
@@ -756,6 +763,7 @@ int zero_state(sesnt_t *h) {
         {h->vc, h->kahan ? E * 3 * (size_t)h->nuni * h->S : 0},
         {h->F, E * 3 * (size_t)h->nuni * h->S},
         {h->F64, h->F64 ? 8 * 3 * (size_t)h->nuni * h->S : 0},
+        {h->sigc, h->sigc ? E * 6 * (size_t)h->state_cs() * h->nel * h->S : 0},
         {h->d_seis, E * (size_t)h->S * h->rec_elem.size() * 3 * h->g.nt},
         {h->d_xseis, E * (size_t)h->S * h->nxtr * h->g.nt},
         {h->du, E * 9 * (size_t)h->nloc * h->S},
@@ -1744,6 +1752,8 @@ size_t footprint(const sesnt_grid_t *g, bool aniso) {
     b += nel * state_unit((int)NP, g->n_sls ? kNsls : 0) * E * S;  // sigma and memory variables (StateLayout)
     b += nuni * E * (1 + S * (6 + ((g->flags & SESNT_FLAG_KAHAN) ? 3 : 0)));  // invM, v, F, comp
     if ((g->flags & SESNT_FLAG_FORCE64) && E == 4) b += nuni * 8 * 3 * S;     // FP64 force
+    if (g->flags & SESNT_FLAG_KAHAN_STRESS)                                     // stress compensation
+        b += nel * 6 * (size_t)state_cs((int)NP, g->n_sls != 0) * E * S;
     b += nloc * E * S * (((g->flags & SESNT_FLAG_STRAIN) ? 9 : 0) + ((g->flags & SESNT_FLAG_ROTATION) ? 6 : 0));
     // set_model (transient): a float32 staging slot per model array, and rhoinv in the handle's layout
     b += nloc * (sizeof(float) * (3 + (g->n_sls ? 1 : 0) + (aniso ? 3 : 0)) + E);
@@ -1841,6 +1851,11 @@ int sesnt_create(const sesnt_grid_t *grid, sesnt_t **out) {
     }
     if ((grid->flags & SESNT_FLAG_FORCE64) && !h->dbl &&
         (rc = h->alloc((void **)&h->F64, 3 * nuni * 8 * S, "FP64 force"))) {
+        g_create_error = h->err;
+        return rc;
+    }
+    if ((grid->flags & SESNT_FLAG_KAHAN_STRESS) &&
+        (rc = h->alloc(&h->sigc, 6 * (size_t)h->state_cs() * h->nel * E * S, "stress compensation"))) {
         g_create_error = h->err;
         return rc;
     }

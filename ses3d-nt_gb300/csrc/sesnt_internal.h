@@ -85,6 +85,7 @@ struct StepArgs {
     // state
     T *sig, *mem, *v, *vc, *F;
     double *F64;  // the force in FP64 (SESNT_FLAG_FORCE64 on FP32 handles), or null
+    T *sigc;      // stress compensation terms [units][6][CS] (SESNT_FLAG_KAHAN_STRESS), or null
     const T *invM;
     // sources
     int nsrc, nt;

@@ -36,6 +36,7 @@ FLAG_NO_PAIR = 128
 FLAG_NO_STAGE = 256
 FLAG_AUTOTUNE = 512
 FLAG_FORCE64 = 1024
+FLAG_KAHAN_STRESS = 2048
 (ELEMENT_AUTO, ELEMENT_POINT, ELEMENT_PAIR, ELEMENT_STAGE, ELEMENT_STAGE_REG, ELEMENT_PERSISTENT, ELEMENT_COLUMNS,
  ELEMENT_COLUMNS_STAGED, ELEMENT_COLUMNS_PAIR) = range(9)
 SOURCE_MT, SOURCE_SF = 0, 1

@@ -5,7 +5,8 @@ synchronising call returns as SESNT_ERANGE. This is the stand-in for a
 memory sanitizer: the library is rebuilt with the checks, and a subprocess
 runs every kernel variant (degrees 2-7, elastic and SLS, anisotropy,
 batches, FP32 and FP64, the staged, persistent, column (one and two
-simulations per thread) and tensor-core element kernels, the tuner's sweep, strain and rotation state, every receiver
+simulations per thread) and tensor-core element kernels, compensated stress
+integration, the tuner's sweep, strain and rotation state, every receiver
 channel, snapshot fields, the kinetic energy) on small grids."""
 import os
 import subprocess
@@ -58,6 +59,9 @@ cases = [  # lpd, n_sls, aniso, kind, flags, batch[, (variant, arg, piece) or "t
     (4, 0, False, sesnt.SOURCE_MT, 0, 4, (CP, 9, 0)),
     (7, 0, True, sesnt.SOURCE_SF, 0, 2, (CP, 0, 0)),
     (3, 0, False, sesnt.SOURCE_MT, 0, 6, (CP, 10, 0), 8),
+    (4, 3, False, sesnt.SOURCE_MT, sesnt.FLAG_KAHAN_STRESS, 2),
+    (3, 3, True, sesnt.SOURCE_SF, sesnt.FLAG_KAHAN_STRESS, 1),
+    (6, 0, False, sesnt.SOURCE_MT, sesnt.FLAG_KAHAN_STRESS, 1, None, 8),
 ]
 for case in cases:
     lpd, n_sls, aniso, kind, flags, batch = case[:6]
@@ -108,4 +112,4 @@ def test_every_kernel_in_bounds(gpu, tmp_path):
     code = SCRIPT % (PKG, HERE, str(tmp_path))
     r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=900)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
-    assert "OK 27" in r.stdout
+    assert "OK 30" in r.stdout

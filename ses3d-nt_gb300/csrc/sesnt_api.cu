@@ -391,6 +391,7 @@ struct sesnt_handle {
     cudaGraphExec_t graph = nullptr;
     int graph_steps = 0;
     cudaGraphExec_t graph1 = nullptr;  // one step, for sesnt_step
+    cudaGraphExec_t graph1a = nullptr; // one step that advances the step counter (first runs)
     // graphs of 16, 8, 4 and 2 steps that advance the step counter, for the
     // remainder of a run below kGraphSteps (index log2(steps) - 1), built
     // when a run first needs them
@@ -500,6 +501,8 @@ struct sesnt_handle {
         graph_steps = 0;
         if (graph1) cudaGraphExecDestroy(graph1);
         graph1 = nullptr;
+        if (graph1a) cudaGraphExecDestroy(graph1a);
+        graph1a = nullptr;
         for (cudaGraphExec_t &l : ladder) {
             if (l) cudaGraphExecDestroy(l);
             l = nullptr;
@@ -1089,6 +1092,7 @@ int prebuild_graphs(sesnt_t *h) {
     for (int q = 0; q < sesnt_handle::kLadder; ++q)
         if (!h->ladder[q] && (rc = capture_steps<T>(h, 2 << q, &h->ladder[q], true))) return rc;
     if (!h->graph1 && (rc = capture_steps<T>(h, 1, &h->graph1, false))) return rc;
+    if (!h->graph1a && (rc = capture_steps<T>(h, 1, &h->graph1a, true))) return rc;
     return SESNT_OK;
 }
 
@@ -1098,16 +1102,33 @@ int prebuild_graphs(sesnt_t *h) {
 // A run of 2..31 steps launched directly measured about 15 us per step slower
 // than replayed (config 2: 0.302 against 0.287 ms): the per-step stream
 // fork and join cost more as launches than as graph edges.
+// A chunk whose graph the handle has not captured yet (its first runs)
+// replays a one-step graph instead, which costs a fraction of a 16- or
+// 32-step capture, so the device starts at once; the 32-step graph is
+// captured while the device runs that first chunk, and prebuild_graphs
+// captures the rest after the run's launches.
 template <typename T>
 int run_steps(sesnt_t *h, int it0, int nsteps) {
     int rc;
     k_set_it<<<1, 1, 0, h->stream>>>(h->d_it, it0);
     int left = nsteps;
-    if (h->use_graph && nsteps >= kGraphSteps) {
-        if (!h->graph && (rc = build_graph<T>(h))) return rc;
-        while (left >= kGraphSteps) {
-            cudaError_t e = cudaGraphLaunch(h->graph, h->stream);
+    auto replay1 = [&](int n) -> int {
+        if (!h->graph1a && (rc = capture_steps<T>(h, 1, &h->graph1a, true))) return rc;
+        for (int q = 0; q < n; ++q) {
+            cudaError_t e = cudaGraphLaunch(h->graph1a, h->stream);
             if (e != cudaSuccess) return h->cuda_fail(e, "cudaGraphLaunch");
+        }
+        return SESNT_OK;
+    };
+    if (h->use_graph && nsteps >= kGraphSteps) {
+        while (left >= kGraphSteps) {
+            if (!h->graph) {
+                if ((rc = replay1(kGraphSteps))) return rc;
+                if ((rc = build_graph<T>(h))) return rc;
+            } else {
+                cudaError_t e = cudaGraphLaunch(h->graph, h->stream);
+                if (e != cudaSuccess) return h->cuda_fail(e, "cudaGraphLaunch");
+            }
             left -= kGraphSteps;
             h->mark(it0 + nsteps - left - 1);
         }
@@ -1115,9 +1136,12 @@ int run_steps(sesnt_t *h, int it0, int nsteps) {
     for (int q = sesnt_handle::kLadder - 1; h->use_graph && q >= 0; --q) {
         const int n = 2 << q;  // 16, 8, 4, 2
         if (left < n) continue;
-        if (!h->ladder[q] && (rc = capture_steps<T>(h, n, &h->ladder[q], true))) return rc;
-        cudaError_t e = cudaGraphLaunch(h->ladder[q], h->stream);
-        if (e != cudaSuccess) return h->cuda_fail(e, "cudaGraphLaunch");
+        if (!h->ladder[q]) {
+            if ((rc = replay1(n))) return rc;
+        } else {
+            cudaError_t e = cudaGraphLaunch(h->ladder[q], h->stream);
+            if (e != cudaSuccess) return h->cuda_fail(e, "cudaGraphLaunch");
+        }
         left -= n;
         h->mark(it0 + nsteps - left - 1);
     }

@@ -290,6 +290,29 @@ def test_graph_and_chunked_runs_agree(gpu, sesnt_lib):
     assert rel_l2(b, a) < 1e-5 and rel_l2(c, a) < 1e-5
 
 
+def test_first_and_later_runs_agree(gpu, sesnt_lib):
+    """A handle's first run replays a one-step graph for the chunks whose
+    graphs are not captured yet; later runs replay the 32-step and ladder
+    graphs. In FP64 (where only the order of the atomic adds differs) both
+    equal direct launches, for run lengths that exercise every chunk size."""
+    wl = with_grid(small_workload(4, n_sls=3, nt=300), precision=8)
+    direct, _, _ = run_gpu(with_grid(wl, flags=sesnt.FLAG_NO_GRAPH), 300, fields=())
+    for lengths in ((300,), (31, 1, 63, 205), (2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 37, 41, 93)):
+        with sesnt.Simulation(wl.grid) as sim:
+            workloads.setup(sim, wl)
+            for rep in range(2):  # the first run captures, the second replays
+                if rep:
+                    sim.reset()
+                it = 1
+                for n in lengths:
+                    sim.run(it, n)
+                    it += n
+                assert it == 301
+                e = rel_l2(sim.seismograms(), direct)
+                print("runs %s, pass %d: vs direct launches %.2e" % (lengths, rep, e))
+                assert e < 1e-12
+
+
 @pytest.mark.parametrize("lpd,n_sls,aniso", [(4, 3, False), (4, 0, True), (6, 3, True), (7, 3, False), (2, 0, False)])
 def test_persistent_and_simple_element_kernels_agree(gpu, sesnt_lib, lpd, n_sls, aniso):
     """The persistent prefetching element kernel and the one-block-per-group

@@ -691,8 +691,8 @@ def main():
                     help="skip the batched-against-plain comparison of the default run")
     ap.add_argument("--element", default="tuned",
                     choices=["tuned", "simple", "persistent", "unstaged", "tc_tf32x3", "tc_bf16x3"] +
-                            ["columns:%d" % q for q in range(4)] + ["columns_staged:%d" % q for q in range(4)] +
-                            ["columns_pair:%d" % q for q in (0, 1, 2, 3, 8, 9, 10)],
+                            ["columns:%d" % q for q in range(16)] + ["columns_staged:%d" % q for q in range(16)] +
+                            ["columns_pair:%d" % q for q in range(16)],
                     help="element kernel variant (all compute the full step): tuned = the library's tuner "
                          "picks on this grid; simple = the launch rules; tc_*: tcgen05 contractions")
     args = ap.parse_args()

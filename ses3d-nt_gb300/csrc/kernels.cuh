@@ -294,7 +294,8 @@ __device__ __forceinline__ void stress_rates(T exx, T eyy, T ezz, T exy, T exz, 
 // KS: compensated (Kahan) stress integration (SESNT_FLAG_KAHAN_STRESS): sigc
 // points to the point's six compensation terms (global memory, stride cs),
 // which carry the low-order part the FP32 stress loses at each step. The
-// compensation is tapered with the stress.
+// compensation is tapered with the stress and also takes up the rounding of
+// the taper's product.
 template <int N, typename T, int NSLS, bool ANISO, bool DU = false, bool SMEM = false, bool PM = false,
           bool KS = false>
 __device__ __forceinline__ void point_stress(const StepArgs<T> &a, const T (&e)[9], T vx, T vy, T vz, int i, int j,
@@ -364,8 +365,14 @@ __device__ __forceinline__ void point_stress(const StepArgs<T> &a, const T (&e)[
     put(sig + 4 * cs, syz * tp);
     put(sig + 5 * cs, szz * tp);
     if constexpr (KS) {
+        // the taper's product rounds too: with s' = t*tp as stored, the tapered
+        // sum is s' - (c*tp + (s' - t*tp)), and fma gives t*tp - s' exactly
+        const T o6[6] = {sxx, sxy, sxz, syy, syz, szz};
 #pragma unroll
-        for (int q = 0; q < 6; ++q) st_stream(sigc + q * cs, cn[q] * tp);
+        for (int q = 0; q < 6; ++q) {
+            const T stored = o6[q] * tp;
+            st_stream(sigc + q * cs, cn[q] * tp - fma(o6[q], tp, -stored));
+        }
     }
     if constexpr (NSLS > 0) {
         // memory variables after the update, driven by this step's rates:

@@ -5,7 +5,10 @@ src/examples/ (gll_test.f90, coordinates_test.f90, interpolation_test.f90);
 each is restated here against the oracle. The GLL points and weights are
 further checked against independently computed Gauss-Lobatto-Legendre nodes,
 and the committed golden fixture (tests/golden/, made by
-tests/golden/make_golden.py) freezes the oracle's config-1 output.
+tests/golden/make_golden.py) freezes the oracle's config-1 output. The GLL
+knots and the point coordinates are also checked against output of the
+reference's own Python package (ses3dpy), made by
+tests/golden/make_ses3dpy_golden.py.
 """
 import math
 import os
@@ -45,6 +48,35 @@ def test_gll_points_known_answers(oracle_mod, lpd):
     # it differentiates x exactly
     assert np.allclose(d.sum(axis=0), 0.0, atol=1e-12)
     assert np.allclose(k @ d, 1.0, atol=1e-12)
+
+
+def test_knots_and_coordinates_match_ses3dpy(oracle_mod):
+    """GLL knots and 1-D point coordinates against the reference's own Python
+    package: tests/golden/ses3dpy_geometry.json, made by
+    tests/golden/make_ses3dpy_golden.py with ses3dpy.get_knots and
+    ses3dpy.generate_coordinates. generate_coordinates leaves out the first
+    point of every element (the shared ones, and the very first) and works in
+    float64 from the config's degrees and metres; the oracle's construction is
+    float32, as the reference's Fortran."""
+    import json
+    with open(os.path.join(GOLDEN, "ses3dpy_geometry.json")) as f:
+        d = json.load(f)
+    assert sorted(d["knots"]) == [str(n) for n in range(2, 8)]
+    for lpd, knots in d["knots"].items():
+        k, _, _ = oracle_mod.gll(int(lpd), precision=8)
+        assert np.allclose(k, knots, rtol=0, atol=1e-15), lpd
+        # the float32 tables fold the closed forms in float32 (a few roundings,
+        # pinned exactly by test_gll_float32_matches_float32_closed_forms)
+        k32, _, _ = oracle_mod.gll(int(lpd), precision=4)
+        assert np.allclose(k32, knots, rtol=0, atol=2.5e-7), lpd
+    assert d["configs"]
+    for name, c in d["configs"].items():
+        for axis, key in enumerate(("theta", "phi", "r")):
+            n = c["nX_global"][axis]
+            x = oracle_mod.coordinates_1d(n, c["lpd"], c["minX"][axis], c["maxX"][axis])
+            want = np.asarray(c[key])
+            assert want.size == n * c["lpd"], (name, key)
+            assert np.allclose(x[:, 1:].ravel(), want, rtol=2e-7, atol=0), (name, key)
 
 
 @pytest.mark.parametrize("lpd", range(1, 8))

@@ -226,9 +226,13 @@ def element_kernel_name(element, g):
     --element choice other than tuned/columns (kernels.cuh:plan_element); a
     run reads the kernel it actually launched from the library."""
     import sesnt
+    if g.flags & sesnt.FLAG_KAHAN_STRESS:  # compensated stress: staged (SLS, degrees 4-7) or point kernel
+        return "k_element_stage" if g.n_sls > 0 and g.lpd >= 4 else "k_element"
     if element.startswith("columns"):
         if g.n_sls:
             return element_kernel_name("simple", g)
+        if element.startswith("columns_pair"):
+            return "k_element_cols2" if g.batch >= 2 and g.batch % 2 == 0 else element_kernel_name("simple", g)
         return "k_element_cols (staged stress)" if element.startswith("columns_staged") else "k_element_cols"
     if element.startswith("tc_"):
         return "k_element_tc"
@@ -246,7 +250,7 @@ def graph_launches(K, per_step):
     set at the start, and one counter advance per replayed graph that ends
     before the run does (runs of 32 steps, then graphs of 16, 8, 4 and 2, the
     last single step without an advance; the rules of run_steps in
-    sesnt_api.cu)."""
+    sesnt_api.cu once a handle's graphs exist, as sesnt_run_timed makes sure)."""
     graphs, left = K // 32, K % 32
     for n in (16, 8, 4, 2):
         if left >= n:

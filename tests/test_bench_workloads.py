@@ -28,6 +28,11 @@ def grid(lpd=4, n_sls=3, batch=1, flags=0):
     (dict(lpd=3), "simple", "k_element"),                          # several elements per block
     (dict(flags=sesnt.FLAG_STRAIN), "simple", "k_element"),        # displacement gradient kept
     (dict(n_sls=0, batch=64), "simple", "k_element_pair"),         # config-1 grid, 64 sources
+    (dict(n_sls=0, batch=64), "columns:5", "k_element_cols"),
+    (dict(n_sls=0, batch=64), "columns_pair:1", "k_element_cols2"),
+    (dict(n_sls=0, batch=3), "columns_pair:1", "k_element"),       # odd batch: no simulation pairs
+    (dict(flags=sesnt.FLAG_KAHAN_STRESS), "simple", "k_element_stage"),
+    (dict(n_sls=0, batch=2, flags=sesnt.FLAG_KAHAN_STRESS), "simple", "k_element"),
 ])
 def test_element_kernel_name(kw, element, kernel):
     assert bench.element_kernel_name(element, grid(**kw)) == kernel

@@ -319,8 +319,9 @@ int sesnt_get_samples(sesnt_t *h, int it, float *out);
 /* Checkpoint and resume (no counterpart in the reference, which keeps no
  * restartable state). sesnt_state_bytes gives the size of the host buffer;
  * sesnt_save_state copies the time-stepping state into it: velocity,
- * stress, memory variables, Kahan compensation, displacement gradient, the
- * recorded traces and the last step. sesnt_load_state restores it into a
+ * stress, memory variables, the compensation terms of the velocity and of the
+ * stress (SESNT_FLAG_KAHAN, SESNT_FLAG_KAHAN_STRESS), displacement gradient,
+ * the recorded traces and the last step. sesnt_load_state restores it into a
  * handle with the same grid, precision, flags and receivers (model and
  * sources are not part of the state), after which stepping continues at
  * the saved step + 1. Synchronous. */

@@ -2316,6 +2316,7 @@ std::vector<std::pair<void *, size_t>> state_buffers(sesnt_t *h) {
     // stress with the memory variables (StateLayout)
     std::vector<std::pair<void *, size_t>> b = {{h->v, 3 * nuni * E * S}, {h->sig, h->state_unit() * nel * E * S}};
     if (h->vc) b.push_back({h->vc, 3 * nuni * E * S});
+    if (h->sigc) b.push_back({h->sigc, 6 * (size_t)h->state_cs() * nel * E * S});  // stress compensation
     if (h->du) b.push_back({h->du, 9 * (size_t)h->nloc * E * S});
     if (h->d_seis) b.push_back({h->d_seis, S * h->rec_elem.size() * 3 * (size_t)h->g.nt * E});
     if (h->d_xseis) b.push_back({h->d_xseis, S * (size_t)h->nxtr * h->g.nt * E});
@@ -2333,7 +2334,7 @@ StateHeader state_header(const sesnt_t *h) {
     std::memcpy(hd.magic, "SESNTST1", 8);
     hd.nx = h->g.nx; hd.ny = h->g.ny; hd.nz = h->g.nz; hd.lpd = h->g.lpd; hd.batch = h->S;
     hd.precision = h->g.precision; hd.n_sls = h->g.n_sls; hd.nrec = (int)h->rec_elem.size(); hd.nxtr = h->nxtr;
-    hd.flags = h->g.flags & (SESNT_FLAG_KAHAN | SESNT_FLAG_STRAIN);
+    hd.flags = h->g.flags & (SESNT_FLAG_KAHAN | SESNT_FLAG_KAHAN_STRESS | SESNT_FLAG_STRAIN);
     hd.last_it = h->last_it;
     return hd;
 }

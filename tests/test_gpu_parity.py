@@ -626,7 +626,7 @@ def test_model_validation(gpu, sesnt_lib):
             sim.set_model(m["rhoinv"], m["lambda"], m["mu"], q=q)  # elastic handle, q given
 
 
-@pytest.mark.parametrize("flags", [0, sesnt.FLAG_KAHAN | sesnt.FLAG_STRAIN])
+@pytest.mark.parametrize("flags", [0, sesnt.FLAG_KAHAN | sesnt.FLAG_STRAIN, sesnt.FLAG_KAHAN_STRESS])
 def test_checkpoint_and_resume(gpu, sesnt_lib, flags):
     """A state saved after step 60 and loaded into a fresh handle continues
     to the same seismograms and wavefields as the uninterrupted run."""
@@ -650,6 +650,28 @@ def test_checkpoint_and_resume(gpu, sesnt_lib, flags):
         with pytest.raises(sesnt.SesntError) as e:
             sim.load_state(ck)
         assert e.value.code == sesnt.EINVAL
+
+
+def test_checkpoint_holds_the_stress_compensation(gpu, sesnt_lib):
+    """A handle with compensated stress integration saves its six
+    compensation terms per point with the state, and its checkpoints load
+    only into handles with the same flag."""
+    wl = small_workload(4, n_sls=3, nt=40)
+    ks = with_grid(wl, flags=sesnt.FLAG_KAHAN_STRESS)
+    cks = []
+    for w in (wl, ks):
+        with sesnt.Simulation(w.grid) as sim:
+            workloads.setup(sim, w)
+            sim.run(1, 20)
+            cks.append(sim.save_state())
+    cs = 125  # the state layout's component stride of visco-elastic degree 4 (unpadded)
+    assert len(cks[1]) - len(cks[0]) == 6 * cs * wl.grid.nx * wl.grid.ny * wl.grid.nz * 4
+    for w, ck in ((wl, cks[1]), (ks, cks[0])):
+        with sesnt.Simulation(w.grid) as sim:
+            workloads.setup(sim, w)
+            with pytest.raises(sesnt.SesntError) as e:
+                sim.load_state(ck)
+            assert e.value.code == sesnt.EINVAL
 
 
 @pytest.mark.parametrize("lpd,n_sls,batch", [(4, 3, 1), (6, 3, 2), (4, 0, 4), (5, 0, 1)])
